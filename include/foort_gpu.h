@@ -1,0 +1,228 @@
+/*
+ * foort_gpu.h -- C ABI of the GB300 geodesic-integration engine.
+ *
+ * The engine replaces the integration stage of a FOORT run: the OpenMP pixel loop
+ * FOORT/Main.cpp:327-414 and everything it calls (ViewScreen initial conditions,
+ * Geodesic::Reset/Update, the RK4/Verlet integrators, Metric::getChristoffel_udd,
+ * the Terminations and the Diagnostics). One null geodesic per pixel is integrated
+ * backward from the camera until a termination fires.
+ *
+ * Conventions (plain C, no C++ types or exceptions cross this boundary):
+ *   - every function returns FOORT_OK (0) or a negative FOORT_E_* code;
+ *   - buffers are owned by the caller;
+ *   - one context per host thread; a context is not reentrant;
+ *   - foort_gpu_last_error() gives a human-readable message for the last failure.
+ *
+ * The enum values, bitflags and termination codes are numerically identical to the
+ * reference's, so a FOORT host that already holds TermBitflag / DiagBitflag values can
+ * pass them through unchanged:
+ *   Terminations.h:29-33 (TermBitflag), Terminations.h:48-67 (enum class Term),
+ *   Diagnostics.h:33-37 (DiagBitflag).
+ */
+#ifndef FOORT_GPU_H
+#define FOORT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ---------------------------------------------------------------- */
+#define FOORT_OK 0
+#define FOORT_E_BADARG (-1)      /* invalid descriptor, pointer or size               */
+#define FOORT_E_CUDA (-2)        /* a CUDA runtime call failed                         */
+#define FOORT_E_BUDGET (-3)      /* the global step budget ran out; results partial   */
+#define FOORT_E_NUMERIC (-4)     /* at least one geodesic hit a non-finite state       */
+#define FOORT_E_CANCELLED (-5)   /* foort_gpu_cancel() stopped the launch             */
+#define FOORT_E_UNSUPPORTED (-6) /* option combination this build does not implement  */
+
+/* ---- plugin ids ------------------------------------------------------------------ */
+/* Metric classes of Metric.h:78-189; the names follow Config.cpp:153-290. */
+#define FOORT_METRIC_KERR 0           /* params: a                                   */
+#define FOORT_METRIC_FLAT 1           /* params: none                                */
+#define FOORT_METRIC_RASHEED_LARSEN 2 /* params: m, a, p, q                          */
+#define FOORT_METRIC_JOHANNSEN 3      /* params: a, alpha13, alpha22, alpha52, eps3  */
+#define FOORT_METRIC_MANKO_NOVIKOV 4  /* params: a, alpha3                           */
+
+/* GeodesicIntegratorFunc choices, Integrators.h:240-248 */
+#define FOORT_INTEGRATOR_RK4 0
+#define FOORT_INTEGRATOR_VERLET 1
+
+/* Arithmetic of the integration kernel */
+#define FOORT_PREC_FP64 0  /* every operation in FP64, finite-difference Christoffels   */
+#define FOORT_PREC_MIXED 1 /* FP32 bulk with compensated state, FP64 where needed       */
+
+/* TermBitflag, Terminations.h:29-33 */
+#define FOORT_TERM_BOUNDARY_SPHERE 0x1u
+#define FOORT_TERM_TIMEOUT 0x2u
+#define FOORT_TERM_HORIZON 0x4u
+#define FOORT_TERM_THETA_SINGULARITY 0x8u
+
+/* DiagBitflag, Diagnostics.h:33-37 */
+#define FOORT_DIAG_GEODESIC_POSITION 0x1u
+#define FOORT_DIAG_FOUR_COLOR_SCREEN 0x2u
+#define FOORT_DIAG_EQUATORIAL_PASSES 0x4u
+#define FOORT_DIAG_CLOSEST_RADIUS 0x8u
+
+/* enum class Term, Terminations.h:48-67 */
+#define FOORT_TERMCODE_CONTINUE 0
+#define FOORT_TERMCODE_HORIZON 1
+#define FOORT_TERMCODE_BOUNDARY_SPHERE 2
+#define FOORT_TERMCODE_TIMEOUT 3
+#define FOORT_TERMCODE_THETA_SINGULARITY 4
+
+/* Per-geodesic error bits (engine extension; the reference has no such report). */
+#define FOORT_ERR_NONFINITE 0x1u   /* state became NaN/Inf; integration stopped      */
+#define FOORT_ERR_VERLET_ITER 0x2u /* Verlet velocity iteration hit its cap           */
+#define FOORT_ERR_BUDGET 0x4u      /* stopped by the global step budget (term = 0)    */
+#define FOORT_ERR_CANCELLED 0x8u   /* stopped by foort_gpu_cancel (term = 0)          */
+#define FOORT_ERR_UNFINISHED 0x10u /* never started (launch stopped before it)        */
+
+/* Diagnostic update cadence, Diagnostics.h:50-55 (UpdateFrequency). */
+typedef struct foort_update_freq {
+    uint64_t every_n; /* >0: update every n steps; 0: only at start and/or finish */
+    int32_t at_start;
+    int32_t at_finish;
+} foort_update_freq;
+
+/* One image: a metric instance plus a camera (ViewScreen.h:44-51). */
+typedef struct foort_image_desc {
+    double metric_params[6]; /* see FOORT_METRIC_* for the order                    */
+    double cam_pos[4];       /* (t, r, theta, phi); r is the ordinary radius         */
+    double cam_dir[4];       /* only {0,-1,0,0} is supported, as in the reference     */
+    double screen_size[2];
+    double screen_center[2];
+} foort_image_desc;
+
+/*
+ * Everything the reference holds in process globals during a round (Main.cpp:211-235,
+ * Config.cpp:11-28, Integrators.h:31-57), as one POD descriptor.
+ */
+typedef struct foort_run_desc {
+    int32_t metric_id;     /* FOORT_METRIC_*                                         */
+    int32_t rlog;          /* RLogScale: integrate u = ln r (Metric.cpp:134)         */
+    int32_t integrator_id; /* FOORT_INTEGRATOR_*                                      */
+    int32_t precision;     /* FOORT_PREC_*                                            */
+
+    double epsilon;        /* Integrators::epsilon, default 0.03                     */
+    double derivative_h;   /* Integrators::Derivative_hval, default 1e-7             */
+    double smallest_step;  /* Integrators::SmallestPossibleStepsize, default 1e-12   */
+    double verlet_tol;     /* Integrators::VerletVelocityTolerance, default 0.001    */
+
+    uint32_t term_flags;   /* FOORT_TERM_* bitflag                                    */
+    uint32_t diag_flags;   /* FOORT_DIAG_* bitflag                                    */
+    uint32_t value_diag;   /* the one diagnostic whose value feeds the Mesh           */
+    uint32_t reserved0;
+
+    double horizon_eps;          /* HorizonTermOptions::AtHorizonEps (relative)      */
+    uint64_t horizon_every;      /* UpdateEveryNSteps                                 */
+    double boundary_radius;      /* BoundarySphereTermOptions::SphereRadius          */
+    uint64_t boundary_every;
+    uint64_t timeout_max_steps;  /* TimeOutTermOptions::MaxSteps                     */
+    uint64_t timeout_every;
+    double theta_eps;            /* ThetaSingularityTermOptions::ThetaSingEpsilon    */
+    uint64_t theta_every;
+
+    foort_update_freq equat_freq;     /* EquatorialPassesOptions                      */
+    double equat_threshold;
+    foort_update_freq closest_freq;   /* ClosestRadiusOptions                         */
+    foort_update_freq geopos_freq;    /* GeodesicPositionOptions                      */
+    uint64_t geopos_output_steps;
+
+    uint32_t n_images;               /* >= 1                                          */
+    uint32_t reserved1;
+    const foort_image_desc* images;  /* host array of n_images entries                */
+} foort_run_desc;
+
+/* One pixel to integrate. Unit screen point = (row, col) / (grid - 1)
+ * (Mesh.cpp:49 SimpleSquareMesh, Mesh.cpp:671-672 SquareSubdivisionMeshV2). */
+typedef struct foort_pixel {
+    uint32_t image;
+    uint32_t reserved;
+    uint64_t row;
+    uint64_t col;
+    uint64_t grid;
+} foort_pixel;
+
+/* Per-geodesic result: the state Geodesic.h:114-122 ends with plus every diagnostic. */
+typedef struct foort_result {
+    int32_t term;          /* FOORT_TERMCODE_*                                       */
+    uint32_t err;          /* FOORT_ERR_* bits                                       */
+    uint64_t steps;        /* Geodesic::Update calls                                 */
+    double lambda;         /* final affine parameter                                 */
+    double pos[4];
+    double vel[4];
+    int32_t quadrant;      /* FourColorScreen (Diagnostics.cpp:159-200)              */
+    int32_t equat_passes;  /* EquatorialPasses (Diagnostics.cpp:351-380)             */
+    double closest_r;      /* ClosestRadius (Diagnostics.cpp:427-446)                */
+} foort_result;
+
+/* Counters of the last launch. */
+typedef struct foort_stats {
+    uint64_t geodesics;      /* geodesics finished                                  */
+    uint64_t steps;          /* integration steps summed over geodesics             */
+    uint64_t rhs_evals;      /* right-hand-side evaluations (Verlet iterations incl.) */
+    uint64_t fp64_steps;     /* mixed kernel: steps taken on the FP64 path           */
+    double kernel_ms;        /* device time of the last launch (CUDA events)         */
+    uint32_t status;         /* FOORT_OK or the launch's FOORT_E_* code             */
+    uint32_t n_blocks;
+    uint32_t block_size;
+    uint32_t reserved;
+} foort_stats;
+
+typedef struct foort_ctx foort_ctx;
+
+/* Fill a descriptor with the reference's defaults (Config.cpp:127-1071): Kerr a=0.5,
+ * RK4 eps=0.03, h=1e-7, hmin=1e-12, Verlet tol 1e-3, Boundary 1000 + TimeOut 1e4,
+ * FourColorScreen as value diagnostic. `images` must be set by the caller. */
+void foort_gpu_default_desc(foort_run_desc* desc);
+
+/* Validate the descriptor, build the per-image camera frames (ViewScreen.cpp:10-73)
+ * and the device-side constants. Replaces the object construction of Main.cpp:211-235. */
+int foort_gpu_create(const foort_run_desc* desc, foort_ctx** out_ctx);
+
+/* Integrate n pixels held in HOST memory and write n results to HOST memory.
+ * Synchronous. Replaces one round of Main.cpp:348-402 (SetNewInitialConditions,
+ * Geodesic::Reset, the Update loop, getDiagnosticFinalValue/getAllOutputStr). */
+int foort_gpu_integrate(foort_ctx* ctx, const foort_pixel* px, uint64_t n, foort_result* out);
+
+/* Same with DEVICE buffers, enqueued on `cuda_stream` (a cudaStream_t, 0 = legacy).
+ * Returns once the launch is enqueued; foort_gpu_sync() waits and reports status. */
+int foort_gpu_integrate_async(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n,
+                              foort_result* d_out, void* cuda_stream);
+
+/* Wait for the last async launch of this context and return its status. */
+int foort_gpu_sync(foort_ctx* ctx);
+
+/* Global budget of integration steps per launch (0 = unlimited). When it runs out the
+ * kernel stops every lane, marks unfinished results with FOORT_ERR_BUDGET and the
+ * launch returns FOORT_E_BUDGET. The reference has only the per-geodesic TimeOut
+ * (Terminations.cpp:159-186). */
+int foort_gpu_set_budget(foort_ctx* ctx, uint64_t max_total_steps);
+
+/* Ask the running launch to stop (host flag in mapped pinned memory, polled by the
+ * kernel every few hundred steps). Safe to call from another host thread. */
+int foort_gpu_cancel(foort_ctx* ctx);
+
+/* Launch shape override (0 = autotuned default). */
+int foort_gpu_set_launch(foort_ctx* ctx, uint32_t block_size, uint32_t blocks_per_sm);
+
+int foort_gpu_get_stats(const foort_ctx* ctx, foort_stats* stats);
+
+void foort_gpu_destroy(foort_ctx* ctx);
+
+/* Message of the last failure of this context (or of the last failed create when
+ * ctx is NULL). Never NULL. */
+const char* foort_gpu_last_error(const foort_ctx* ctx);
+
+/* Horizon radius the reference gives the metric (Metric.cpp:113, 250, 385, 496);
+ * 0 for flat space. */
+double foort_horizon_radius(int32_t metric_id, const double* metric_params);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FOORT_GPU_H */
