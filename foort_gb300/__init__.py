@@ -1,0 +1,161 @@
+"""GB300 geodesic-integration engine for FOORT runs.
+
+The compute path is the C-ABI library ``libfoort_gpu.so`` (hand-written sm_103a CUDA
+kernels plus a C++ host layer; see include/foort_gpu.h). This package loads it with
+ctypes and offers a thin Python view used by tests and benchmarks. There is no CPU
+fallback: without the compiled library every entry point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfoort_gpu.so")
+
+_LIB = None
+
+
+class FoortError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"FOORT error {code}: {msg}")
+        self.code = code
+
+
+def load():
+    """Load libfoort_gpu.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise FoortError(abi.FOORT_E_CUDA, f"{LIB_PATH} is missing: build it with foort_gb300.build.build()")
+    lib = C.CDLL(LIB_PATH)
+    vp, u64, i32, u32 = C.c_void_p, C.c_uint64, C.c_int32, C.c_uint32
+    lib.foort_gpu_default_desc.argtypes = [C.POINTER(abi.RunDesc)]
+    lib.foort_gpu_default_desc.restype = None
+    lib.foort_gpu_create.argtypes = [C.POINTER(abi.RunDesc), C.POINTER(vp)]
+    lib.foort_gpu_integrate.argtypes = [vp, vp, u64, vp]
+    lib.foort_gpu_integrate_async.argtypes = [vp, vp, u64, vp, vp]
+    lib.foort_gpu_sync.argtypes = [vp]
+    lib.foort_gpu_set_budget.argtypes = [vp, u64]
+    lib.foort_gpu_cancel.argtypes = [vp]
+    lib.foort_gpu_set_launch.argtypes = [vp, u32, u32]
+    lib.foort_gpu_get_stats.argtypes = [vp, C.POINTER(abi.Stats)]
+    lib.foort_gpu_destroy.argtypes = [vp]
+    lib.foort_gpu_destroy.restype = None
+    lib.foort_gpu_last_error.argtypes = [vp]
+    lib.foort_gpu_last_error.restype = C.c_char_p
+    lib.foort_horizon_radius.argtypes = [i32, vp]
+    lib.foort_horizon_radius.restype = C.c_double
+    lib.foort_abi_size.argtypes = [i32]
+    lib.foort_abi_size.restype = u64
+    lib.foort_measure_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.foort_gpu_has_kernel.argtypes = [i32, i32, i32]
+    _LIB = lib
+    return lib
+
+
+def check_layout():
+    """Compare the ctypes layouts with the compiled library's struct sizes."""
+    lib = load()
+    want = [C.sizeof(abi.Pixel), C.sizeof(abi.Result), C.sizeof(abi.RunDesc), C.sizeof(abi.ImageDesc),
+            C.sizeof(abi.Stats)]
+    got = [lib.foort_abi_size(i) for i in range(5)]
+    if want != got:
+        raise FoortError(abi.FOORT_E_BADARG, f"ABI layout mismatch: python {want} vs library {got}")
+    return got
+
+
+def mixed_available(metric_id=abi.METRIC_KERR, integrator=abi.INTEGRATOR_RK4):
+    """True when this build has a mixed-precision kernel for the metric / integrator."""
+    return bool(load().foort_gpu_has_kernel(metric_id, integrator, abi.PREC_MIXED))
+
+
+def measure_peaks():
+    """Measured FP32 / FP64 FMA throughput of the current GPU in TFLOP/s."""
+    a, b = C.c_double(), C.c_double()
+    rc = load().foort_measure_peaks(C.byref(a), C.byref(b))
+    if rc != 0:
+        raise FoortError(rc, "peak measurement failed")
+    return a.value, b.value
+
+
+class Engine:
+    """One engine context (include/foort_gpu.h: foort_gpu_create ... foort_gpu_destroy)."""
+
+    def __init__(self, desc):
+        self._lib = load()
+        self._desc = desc
+        self._ctx = C.c_void_p()
+        rc = self._lib.foort_gpu_create(C.byref(desc), C.byref(self._ctx))
+        if rc != 0:
+            raise FoortError(rc, self._lib.foort_gpu_last_error(None).decode())
+
+    def _check(self, rc, ok=(0,)):
+        if rc not in ok:
+            raise FoortError(rc, self._lib.foort_gpu_last_error(self._ctx).decode())
+        return rc
+
+    def integrate(self, px, out=None, allow=(0,)):
+        """Host pixels (PIXEL_DTYPE array) -> host results (RESULT_DTYPE array)."""
+        px = np.ascontiguousarray(px, dtype=abi.PIXEL_DTYPE)
+        if out is None:
+            out = np.zeros(len(px), dtype=abi.RESULT_DTYPE)
+        rc = self._lib.foort_gpu_integrate(self._ctx, px.ctypes.data, len(px), out.ctypes.data)
+        self._check(rc, allow)
+        return out
+
+    def integrate_ptr(self, px_ptr, n, out_ptr, allow=(0,)):
+        """Same with raw host pointers (e.g. pinned buffers)."""
+        rc = self._lib.foort_gpu_integrate(self._ctx, C.c_void_p(px_ptr), n, C.c_void_p(out_ptr))
+        return self._check(rc, allow)
+
+    def integrate_async(self, d_px, n, d_out, stream=0):
+        """Device pointers; enqueued on `stream` (a cudaStream_t as int)."""
+        rc = self._lib.foort_gpu_integrate_async(self._ctx, C.c_void_p(d_px), n, C.c_void_p(d_out),
+                                                 C.c_void_p(stream))
+        return self._check(rc)
+
+    def sync(self, allow=(0,)):
+        return self._check(self._lib.foort_gpu_sync(self._ctx), allow)
+
+    def set_budget(self, steps):
+        self._check(self._lib.foort_gpu_set_budget(self._ctx, steps))
+
+    def cancel(self):
+        self._check(self._lib.foort_gpu_cancel(self._ctx))
+
+    def set_launch(self, block_size=0, blocks_per_sm=0):
+        self._check(self._lib.foort_gpu_set_launch(self._ctx, block_size, blocks_per_sm))
+
+    def stats(self):
+        s = abi.Stats()
+        self._lib.foort_gpu_get_stats(self._ctx, C.byref(s))
+        return {k: getattr(s, k) for k, _ in abi.Stats._fields_}
+
+    def last_error(self):
+        return self._lib.foort_gpu_last_error(self._ctx).decode()
+
+    def close(self):
+        if self._ctx:
+            self._lib.foort_gpu_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def horizon_radius(metric_id, params):
+    arr = (C.c_double * 6)(*([float(p) for p in params] + [0.0] * (6 - len(params))))
+    return load().foort_horizon_radius(metric_id, C.cast(arr, C.c_void_p))

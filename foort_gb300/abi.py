@@ -66,6 +66,7 @@ class ImageDesc(C.Structure):
         ("cam_dir", C.c_double * 4),
         ("screen_size", C.c_double * 2),
         ("screen_center", C.c_double * 2),
+        ("horizon_eps", C.c_double),
     ]
 
 
@@ -151,7 +152,7 @@ assert RESULT_DTYPE.itemsize == C.sizeof(Result)
 
 
 def make_image(metric_params=(0.5,), r=1000.0, theta=np.pi / 2, phi=0.0, half_width=10.0, center=(0.0, 0.0),
-               size=None):
+               size=None, horizon_eps=0.0):
     """One image: metric parameters plus a camera at (0, r, theta, phi) looking inward."""
     im = ImageDesc()
     for i, p in enumerate(metric_params):
@@ -162,6 +163,7 @@ def make_image(metric_params=(0.5,), r=1000.0, theta=np.pi / 2, phi=0.0, half_wi
         size = (2.0 * half_width, 2.0 * half_width)
     im.screen_size[:] = [float(size[0]), float(size[1])]
     im.screen_center[:] = [float(center[0]), float(center[1])]
+    im.horizon_eps = float(horizon_eps)
     return im
 
 

@@ -1,0 +1,478 @@
+// Host library of the geodesic engine: the C ABI of include/foort_gpu.h.
+//
+// Per context: the run options (RunConst), the per-image constants (ImageConst, with
+// the camera frame of ViewScreen::ConstructVielbein), a stream, a small block of
+// device counters (work-queue head, step/RHS counters, status) and a cancel flag in
+// mapped pinned host memory. A launch is one persistent kernel over all pixels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "kernels.h"
+
+using namespace foort;
+
+struct foort_ctx {
+    foort_run_desc desc{};
+    std::vector<foort_image_desc> images;
+    RunConst rc{};
+    std::vector<ImageConst> hic;
+    ImageConst* d_images = nullptr;
+    unsigned long long* d_ctr = nullptr;
+    unsigned long long h_ctr[kNumCtr] = {};
+    int32_t* h_cancel = nullptr;
+    int32_t* d_cancel = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaStream_t last_stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    foort_pixel* d_px = nullptr;
+    foort_result* d_out = nullptr;
+    uint64_t cap = 0;
+    uint64_t budget = 0;
+    uint64_t last_n = 0;
+    uint32_t block_size = 0, blocks_per_sm = 0;
+    int device = 0, num_sms = 0;
+    bool pending = false;
+    foort_stats stats{};
+    std::string err;
+};
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err = "no error";
+
+int fail(foort_ctx* c, int code, const std::string& msg) {
+    if (c) {
+        c->err = msg;
+    } else {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        g_create_err = msg;
+    }
+    return code;
+}
+
+int cuda_fail(foort_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, FOORT_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);   \
+    } while (0)
+
+// ViewScreen::ConstructVielbein (ViewScreen.cpp:10-73), in FP64 on the host, with the
+// reference's dense loops so that the frame is the reference's to the last bit.
+void camera_frame(int metric_id, bool rlog, const foort_image_desc& im, ImageConst& ic) {
+    double p[4] = {im.cam_pos[0], im.cam_pos[1], im.cam_pos[2], im.cam_pos[3]};
+    p[1] = rlog ? std::log(p[1]) : p[1];
+    const double r = rlog ? std::exp(p[1]) : p[1];
+    const double s = std::sin(p[2]), c = std::cos(p[2]);
+    G5 a = metric_dd_host(metric_id, ic.m, r, s, c, rlog);
+    G5 b = metric_uu_host(metric_id, ic.m, r, s, c, rlog);
+    double gdd[4][4] = {}, guu[4][4] = {};
+    gdd[0][0] = a.tt; gdd[0][3] = gdd[3][0] = a.tp; gdd[1][1] = a.rr; gdd[2][2] = a.hh; gdd[3][3] = a.pp;
+    guu[0][0] = b.tt; guu[0][3] = guu[3][0] = b.tp; guu[1][1] = b.rr; guu[2][2] = b.hh; guu[3][3] = b.pp;
+    auto ip = [&gdd](const double* u, const double* w) {
+        double acc = 0;
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) acc += u[i] * gdd[i][j] * w[j];
+        return acc;
+    };
+    double e[4][4] = {};
+    double sg[4] = {};
+    auto scale = [](double* v, double f) { for (int i = 0; i < 4; ++i) v[i] = v[i] * f; };
+    // t leg
+    for (int i = 0; i < 4; ++i) e[0][i] = guu[0][i];
+    double n = ip(e[0], e[0]);
+    sg[0] = (n < 0) ? -1 : 1;
+    scale(e[0], sg[0]);
+    scale(e[0], 1 / std::sqrt(sg[0] * n));
+    // phi leg
+    double f0 = sg[0] * ip(guu[3], e[0]);
+    for (int i = 0; i < 4; ++i) e[3][i] = guu[3][i] - e[0][i] * f0;
+    n = ip(e[3], e[3]);
+    sg[3] = (n < 0) ? -1 : 1;
+    scale(e[3], sg[3] * im.cam_pos[1] * std::sin(im.cam_pos[2]));
+    scale(e[3], 1 / std::sqrt(sg[3] * n));
+    // r leg
+    f0 = sg[0] * ip(guu[1], e[0]);
+    double f3 = sg[3] * ip(guu[1], e[3]);
+    for (int i = 0; i < 4; ++i) e[1][i] = (guu[1][i] - e[0][i] * f0) - e[3][i] * f3;
+    n = ip(e[1], e[1]);
+    sg[1] = (n < 0) ? -1 : 1;
+    scale(e[1], sg[1]);
+    scale(e[1], 1 / std::sqrt(sg[1] * n));
+    // theta leg: the reference subtracts a multiple of the (still zero) theta leg itself
+    // instead of the phi leg (ViewScreen.cpp:56-58); kept as written.
+    f0 = sg[0] * ip(guu[2], e[0]);
+    f3 = sg[3] * ip(guu[2], e[3]);
+    double prev2[4] = {e[2][0], e[2][1], e[2][2], e[2][3]};
+    for (int i = 0; i < 4; ++i) e[2][i] = (guu[2][i] - e[0][i] * f0) - prev2[i] * f3;
+    n = ip(e[2], e[2]);
+    sg[2] = (n < 0) ? -1 : 1;
+    scale(e[2], sg[2] * im.cam_pos[1]);
+    scale(e[2], 1 / std::sqrt(sg[2] * n));
+    for (int j = 0; j < 4; ++j)
+        for (int i = 0; i < 4; ++i) ic.e[j][i] = e[j][i];
+    for (int i = 0; i < 4; ++i) ic.gdd0[i] = gdd[0][i];
+    for (int i = 0; i < 4; ++i) ic.pos0[i] = im.cam_pos[i];
+    ic.pos0[1] = p[1];
+    ic.R0 = im.cam_pos[1];
+    ic.sin_th0 = std::sin(p[2]);
+    ic.size[0] = im.screen_size[0];
+    ic.size[1] = im.screen_size[1];
+    ic.center[0] = im.screen_center[0];
+    ic.center[1] = im.screen_center[1];
+}
+
+int validate(const foort_run_desc* d, std::string& why) {
+    if (!d) { why = "descriptor is NULL"; return FOORT_E_BADARG; }
+    if (d->metric_id < 0 || d->metric_id > 4) { why = "unknown metric_id"; return FOORT_E_BADARG; }
+    if (d->integrator_id != FOORT_INTEGRATOR_RK4 && d->integrator_id != FOORT_INTEGRATOR_VERLET) {
+        why = "unknown integrator_id";
+        return FOORT_E_BADARG;
+    }
+    if (d->precision != FOORT_PREC_FP64 && d->precision != FOORT_PREC_MIXED) { why = "unknown precision"; return FOORT_E_BADARG; }
+    if (d->n_images == 0 || !d->images) { why = "no images"; return FOORT_E_BADARG; }
+    if (d->term_flags == 0) { why = "no terminations turned on"; return FOORT_E_BADARG; }
+    if (d->term_flags & ~0xFu) { why = "unknown termination flag"; return FOORT_E_BADARG; }
+    if (d->diag_flags & ~0xFu) { why = "unknown diagnostic flag"; return FOORT_E_BADARG; }
+    if (d->diag_flags & FOORT_DIAG_GEODESIC_POSITION) {
+        why = "GeodesicPosition needs per-step storage, which this entry point does not provide";
+        return FOORT_E_UNSUPPORTED;
+    }
+    if (!(d->epsilon > 0.0) || !(d->derivative_h > 0.0)) { why = "epsilon and derivative_h must be > 0"; return FOORT_E_BADARG; }
+    for (uint32_t i = 0; i < d->n_images; ++i) {
+        const foort_image_desc& im = d->images[i];
+        if (!(im.cam_pos[1] > 0.0)) { why = "camera radius must be > 0"; return FOORT_E_BADARG; }
+    }
+    return FOORT_OK;
+}
+
+RunConst make_run_const(const foort_run_desc& d) {
+    RunConst R{};
+    R.metric_id = d.metric_id;
+    // Flat space is not a SphericalHorizonMetric: no log-r scale (ViewScreen.h:49-50)
+    // and no Horizon termination (Config.cpp:649-657).
+    R.rlog = (d.rlog && d.metric_id != kFlat) ? 1 : 0;
+    R.integrator = d.integrator_id;
+    R.precision = d.precision;
+    R.eps = d.epsilon;
+    R.hfd = d.derivative_h;
+    R.hmin = d.smallest_step;
+    R.vtol = d.verlet_tol;
+    R.term_flags = d.term_flags;
+    if (d.metric_id == kFlat) R.term_flags &= ~FOORT_TERM_HORIZON;
+    R.diag_flags = d.diag_flags;
+    R.h_eps = d.horizon_eps;
+    R.h_every = d.horizon_every;
+    R.b_rad = d.boundary_radius;
+    R.b_every = d.boundary_every;
+    R.t_max = d.timeout_max_steps;
+    R.t_every = d.timeout_every;
+    R.th_eps = d.theta_eps;
+    R.th_every = d.theta_every;
+    R.eq_every = d.equat_freq.every_n;
+    R.eq_start = d.equat_freq.at_start;
+    R.eq_finish = d.equat_freq.at_finish;
+    R.eq_thr = d.equat_threshold;
+    R.cr_every = d.closest_freq.every_n;
+    R.cr_start = d.closest_freq.at_start;
+    R.cr_finish = d.closest_freq.at_finish;
+    R.verlet_cap = 1000;
+    R.poll_steps = 512;
+    return R;
+}
+
+const void* select_kernel(const RunConst& R) {
+    return R.precision == FOORT_PREC_MIXED ? mixed_kernel(R.metric_id, R.integrator)
+                                           : fp64_kernel(R.metric_id, R.integrator);
+}
+
+int ensure_capacity(foort_ctx* ctx, uint64_t n) {
+    if (n <= ctx->cap) return FOORT_OK;
+    if (ctx->d_px) cudaFree(ctx->d_px);
+    if (ctx->d_out) cudaFree(ctx->d_out);
+    ctx->d_px = nullptr;
+    ctx->d_out = nullptr;
+    ctx->cap = 0;
+    CK(cudaMalloc(&ctx->d_px, n * sizeof(foort_pixel)));
+    CK(cudaMalloc(&ctx->d_out, n * sizeof(foort_result)));
+    ctx->cap = n;
+    return FOORT_OK;
+}
+
+int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, cudaStream_t st) {
+    const void* fn = select_kernel(ctx->rc);
+    if (!fn) return fail(ctx, FOORT_E_UNSUPPORTED, "no kernel for this metric / integrator / precision");
+    uint32_t bs = ctx->block_size ? ctx->block_size : 128;
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, static_cast<int>(bs), 0));
+    if (per_sm <= 0) return fail(ctx, FOORT_E_CUDA, "kernel does not fit on an SM with this block size");
+    if (ctx->blocks_per_sm) per_sm = std::min<int>(per_sm, static_cast<int>(ctx->blocks_per_sm));
+    uint64_t full = static_cast<uint64_t>(per_sm) * static_cast<uint64_t>(ctx->num_sms);
+    uint64_t need = (n + bs - 1) / bs;
+    uint32_t grid = static_cast<uint32_t>(std::max<uint64_t>(1, std::min(full, need)));
+    *ctx->h_cancel = 0;
+    CK(cudaMemsetAsync(ctx->d_ctr, 0, kNumCtr * sizeof(unsigned long long), st));
+    LaunchArgs A{};
+    A.px = d_px;
+    A.out = d_out;
+    A.n = n;
+    A.images = ctx->d_images;
+    A.n_images = static_cast<uint32_t>(ctx->hic.size());
+    A.ctr = ctx->d_ctr;
+    A.cancel = ctx->d_cancel;
+    A.budget = ctx->budget;
+    if (!A.budget && !(ctx->rc.term_flags & FOORT_TERM_TIMEOUT)) {
+        // Without TimeOut a geodesic may never terminate (the reference would loop
+        // forever); a finite default budget keeps every launch finite.
+        A.budget = std::max<unsigned long long>(100000000ull, 1000000ull * n);
+    }
+    RunConst R = ctx->rc;
+    void* args[2] = {&A, &R};
+    CK(cudaEventRecord(ctx->ev0, st));
+    if (n > 0) CK(cudaLaunchKernel(fn, dim3(grid), dim3(bs), args, 0, st));
+    CK(cudaEventRecord(ctx->ev1, st));
+    CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, kNumCtr * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    ctx->stats.n_blocks = grid;
+    ctx->stats.block_size = bs;
+    ctx->last_n = n;
+    ctx->last_stream = st;
+    ctx->pending = true;
+    return FOORT_OK;
+}
+
+int finish(foort_ctx* ctx) {
+    if (!ctx->pending) return FOORT_OK;
+    ctx->pending = false;
+    CK(cudaStreamSynchronize(ctx->last_stream));
+    CK(cudaGetLastError());
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->stats.kernel_ms = ms;
+    ctx->stats.steps = ctx->h_ctr[kCtrSteps];
+    ctx->stats.rhs_evals = ctx->h_ctr[kCtrRhs];
+    ctx->stats.fp64_steps = ctx->h_ctr[kCtrFp64Steps];
+    ctx->stats.geodesics = ctx->h_ctr[kCtrDone];
+    const unsigned long long st = ctx->h_ctr[kCtrStatus];
+    int rc = FOORT_OK;
+    if (st & kStatusCancelled) rc = fail(ctx, FOORT_E_CANCELLED, "launch cancelled by foort_gpu_cancel");
+    else if (st & kStatusBudget) rc = fail(ctx, FOORT_E_BUDGET, "global step budget exhausted; unfinished geodesics are marked");
+    ctx->stats.status = static_cast<uint32_t>(rc);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+void foort_gpu_default_desc(foort_run_desc* d) {
+    if (!d) return;
+    std::memset(d, 0, sizeof(*d));
+    d->metric_id = FOORT_METRIC_KERR;
+    d->integrator_id = FOORT_INTEGRATOR_RK4;
+    d->precision = FOORT_PREC_FP64;
+    d->epsilon = 0.03;
+    d->derivative_h = 1e-7;
+    d->smallest_step = 1e-12;
+    d->verlet_tol = 0.001;
+    d->term_flags = FOORT_TERM_BOUNDARY_SPHERE | FOORT_TERM_TIMEOUT;
+    d->diag_flags = FOORT_DIAG_FOUR_COLOR_SCREEN;
+    d->value_diag = FOORT_DIAG_FOUR_COLOR_SCREEN;
+    d->horizon_eps = 0.01;
+    d->horizon_every = 1;
+    d->boundary_radius = 1000.0;
+    d->boundary_every = 1;
+    d->timeout_max_steps = 10000;
+    d->timeout_every = 1;
+    d->theta_eps = 1e-5;
+    d->theta_every = 1;
+    d->equat_freq = foort_update_freq{1, 1, 1};
+    d->equat_threshold = 0.01;
+    d->closest_freq = foort_update_freq{1, 1, 1};
+    d->geopos_freq = foort_update_freq{1, 0, 1};
+}
+
+int foort_gpu_create(const foort_run_desc* desc, foort_ctx** out_ctx) {
+    if (!out_ctx) return fail(nullptr, FOORT_E_BADARG, "out_ctx is NULL");
+    *out_ctx = nullptr;
+    std::string why;
+    int v = validate(desc, why);
+    if (v) return fail(nullptr, v, why);
+    foort_ctx* ctx = new foort_ctx();
+    ctx->desc = *desc;
+    ctx->images.assign(desc->images, desc->images + desc->n_images);
+    ctx->desc.images = ctx->images.data();
+    ctx->rc = make_run_const(*desc);
+    ctx->hic.resize(desc->n_images);
+    for (uint32_t i = 0; i < desc->n_images; ++i) {
+        ImageConst& ic = ctx->hic[i];
+        std::memset(&ic, 0, sizeof(ic));
+        ic.m = make_metric_const(desc->metric_id, desc->images[i].metric_params);
+        camera_frame(desc->metric_id, ctx->rc.rlog != 0, desc->images[i], ic);
+        ic.h_eps = desc->images[i].horizon_eps > 0.0 ? desc->images[i].horizon_eps : desc->horizon_eps;
+        if (ctx->rc.precision == FOORT_PREC_MIXED) fill_mixed_constants(desc->metric_id, ic, ctx->rc);
+    }
+    auto bail = [&](int rc) {
+        std::string m = ctx->err;
+        foort_gpu_destroy(ctx);
+        return fail(nullptr, rc, m);
+    };
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaGetDevice"));
+    e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaDeviceGetAttribute"));
+    if (!select_kernel(ctx->rc)) return bail(fail(ctx, FOORT_E_UNSUPPORTED, "no kernel for this metric / integrator / precision"));
+    e = cudaMalloc(&ctx->d_images, ctx->hic.size() * sizeof(ImageConst));
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaMalloc(images)"));
+    e = cudaMemcpy(ctx->d_images, ctx->hic.data(), ctx->hic.size() * sizeof(ImageConst), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaMemcpy(images)"));
+    e = cudaMalloc(&ctx->d_ctr, kNumCtr * sizeof(unsigned long long));
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaMalloc(counters)"));
+    e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_cancel), sizeof(int32_t), cudaHostAllocMapped);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaHostAlloc(cancel)"));
+    *ctx->h_cancel = 0;
+    e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->d_cancel), ctx->h_cancel, 0);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaHostGetDevicePointer(cancel)"));
+    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaStreamCreate"));
+    if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess || (e = cudaEventCreate(&ctx->ev1)) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaEventCreate"));
+    *out_ctx = ctx;
+    return FOORT_OK;
+}
+
+int foort_gpu_integrate(foort_ctx* ctx, const foort_pixel* px, uint64_t n, foort_result* out) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    if (n && (!px || !out)) return fail(ctx, FOORT_E_BADARG, "NULL pixel or result buffer");
+    for (uint64_t i = 0; i < n; ++i)
+        if (px[i].image >= ctx->hic.size() || px[i].grid < 2)
+            return fail(ctx, FOORT_E_BADARG, "pixel " + std::to_string(i) + " has an invalid image index or grid < 2");
+    int rc = finish(ctx);
+    if (rc != FOORT_OK && rc != FOORT_E_BUDGET && rc != FOORT_E_CANCELLED) return rc;
+    if ((rc = ensure_capacity(ctx, n))) return rc;
+    cudaStream_t st = ctx->stream;
+    if (n) CK(cudaMemcpyAsync(ctx->d_px, px, n * sizeof(foort_pixel), cudaMemcpyHostToDevice, st));
+    if ((rc = launch(ctx, ctx->d_px, n, ctx->d_out, st))) return rc;
+    if (n) CK(cudaMemcpyAsync(out, ctx->d_out, n * sizeof(foort_result), cudaMemcpyDeviceToHost, st));
+    return finish(ctx);
+}
+
+int foort_gpu_integrate_async(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out,
+                              void* cuda_stream) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    if (n && (!d_px || !d_out)) return fail(ctx, FOORT_E_BADARG, "NULL pixel or result buffer");
+    int rc = finish(ctx);
+    if (rc != FOORT_OK && rc != FOORT_E_BUDGET && rc != FOORT_E_CANCELLED) return rc;
+    return launch(ctx, d_px, n, d_out, static_cast<cudaStream_t>(cuda_stream));
+}
+
+int foort_gpu_sync(foort_ctx* ctx) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    return finish(ctx);
+}
+
+int foort_gpu_set_budget(foort_ctx* ctx, uint64_t max_total_steps) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    ctx->budget = max_total_steps;
+    return FOORT_OK;
+}
+
+int foort_gpu_cancel(foort_ctx* ctx) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    *reinterpret_cast<volatile int32_t*>(ctx->h_cancel) = 1;
+    return FOORT_OK;
+}
+
+int foort_gpu_set_launch(foort_ctx* ctx, uint32_t block_size, uint32_t blocks_per_sm) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    if (block_size && (block_size % 32 || block_size > 128))
+        return fail(ctx, FOORT_E_BADARG, "block_size must be a multiple of 32 and at most 128");
+    ctx->block_size = block_size;
+    ctx->blocks_per_sm = blocks_per_sm;
+    return FOORT_OK;
+}
+
+int foort_gpu_get_stats(const foort_ctx* ctx, foort_stats* stats) {
+    if (!ctx || !stats) return FOORT_E_BADARG;
+    *stats = ctx->stats;
+    return FOORT_OK;
+}
+
+void foort_gpu_destroy(foort_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->pending && ctx->last_stream) cudaStreamSynchronize(ctx->last_stream);
+    if (ctx->d_px) cudaFree(ctx->d_px);
+    if (ctx->d_out) cudaFree(ctx->d_out);
+    if (ctx->d_images) cudaFree(ctx->d_images);
+    if (ctx->d_ctr) cudaFree(ctx->d_ctr);
+    if (ctx->h_cancel) cudaFreeHost(ctx->h_cancel);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* foort_gpu_last_error(const foort_ctx* ctx) {
+    if (ctx) return ctx->err.c_str();
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    return g_create_err.c_str();
+}
+
+double foort_horizon_radius(int32_t metric_id, const double* metric_params) {
+    if (!metric_params || metric_id < 0 || metric_id > 4) return 0.0;
+    return make_metric_const(metric_id, metric_params).rh;
+}
+
+int foort_gpu_has_kernel(int32_t metric_id, int32_t integrator_id, int32_t precision) {
+    if (metric_id < 0 || metric_id > 4) return 0;
+    if (integrator_id != FOORT_INTEGRATOR_RK4 && integrator_id != FOORT_INTEGRATOR_VERLET) return 0;
+    if (precision == FOORT_PREC_FP64) return fp64_kernel(metric_id, integrator_id) != nullptr;
+    if (precision == FOORT_PREC_MIXED) return mixed_kernel(metric_id, integrator_id) != nullptr;
+    return 0;
+}
+
+// Sizes of the ABI structs, for binding checks (0 pixel, 1 result, 2 run_desc,
+// 3 image_desc, 4 stats).
+uint64_t foort_abi_size(int32_t which) {
+    switch (which) {
+    case 0: return sizeof(foort_pixel);
+    case 1: return sizeof(foort_result);
+    case 2: return sizeof(foort_run_desc);
+    case 3: return sizeof(foort_image_desc);
+    case 4: return sizeof(foort_stats);
+    default: return 0;
+    }
+}
+
+}  // extern "C"
+
+namespace foort {
+
+const void* fp64_kernel_kerr(int);
+const void* fp64_kernel_flat(int);
+const void* fp64_kernel_rl(int);
+const void* fp64_kernel_joh(int);
+const void* fp64_kernel_mn(int);
+
+const void* fp64_kernel(int metric_id, int integ) {
+    switch (metric_id) {
+    case kKerr: return fp64_kernel_kerr(integ);
+    case kFlat: return fp64_kernel_flat(integ);
+    case kRasheedLarsen: return fp64_kernel_rl(integ);
+    case kJohannsen: return fp64_kernel_joh(integ);
+    case kMankoNovikov: return fp64_kernel_mn(integ);
+    default: return nullptr;
+    }
+}
+
+}  // namespace foort

@@ -1,0 +1,85 @@
+// Internal structures shared by the host library and the kernels.
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/foort_gpu.h"
+#include "metric_fp64.cuh"
+
+namespace foort {
+
+// Truncated pi of the reference (Geometry.h:44); every angular test uses it.
+constexpr double kRefPi = 3.1415926535;
+
+// Per-image constants, computed once on the host (ViewScreen.cpp:10-73).
+struct ImageConst {
+    MetricConst m;
+    double e[4][4];     // vielbein rows: e[j][i] = e_j^i
+    double gdd0[4];     // g_dd[0][*] at the camera, for the E = 1 rescaling
+    double pos0[4];     // initial position (r replaced by ln r in log-r mode)
+    double R0;          // camera radius (ordinary r)
+    double sin_th0;     // sin(theta) at the camera
+    double size[2];     // screen size
+    double center[2];   // screen center
+    double h_eps;       // Epsilon_Horizon of this image (relative)
+    // Mixed-precision kernel: FP32 copies of the metric constants and the radius below
+    // which a lane evaluates its right-hand side in FP64.
+    float qf[6];
+    float rhf;
+    double r_fp64;
+};
+
+// Run options (process globals in the reference, Config.cpp:11-28 and
+// Integrators.h:31-57), passed by value to every launch.
+struct RunConst {
+    int32_t metric_id;
+    int32_t rlog;
+    int32_t integrator;
+    int32_t precision;
+    double eps, hfd, hmin, vtol;
+    uint32_t term_flags, diag_flags;
+    double h_eps;
+    uint64_t h_every;
+    double b_rad;
+    uint64_t b_every;
+    uint64_t t_max, t_every;
+    double th_eps;
+    uint64_t th_every;
+    uint64_t eq_every;
+    int32_t eq_start, eq_finish;
+    double eq_thr;
+    uint64_t cr_every;
+    int32_t cr_start, cr_finish;
+    int32_t verlet_cap;   // cap on Verlet velocity iterations (the reference has none)
+    int32_t poll_steps;   // steps between budget / cancel polls
+};
+
+// Scratch counters of one launch (device memory, zeroed before each launch).
+enum Ctr {
+    kCtrHead = 0,      // next pixel index to hand out (work queue)
+    kCtrSteps = 1,     // integration steps, all geodesics
+    kCtrRhs = 2,       // right-hand-side evaluations
+    kCtrFp64Steps = 3, // mixed kernel: steps evaluated on the FP64 path
+    kCtrDone = 4,      // geodesics finished
+    kCtrStatus = 5,    // FOORT_STATUS_* bits
+    kNumCtr = 8
+};
+
+// Status bits written by the kernel.
+constexpr unsigned long long kStatusBudget = 1ull;
+constexpr unsigned long long kStatusCancelled = 2ull;
+constexpr unsigned long long kStatusNonfinite = 4ull;
+
+struct LaunchArgs {
+    const foort_pixel* px;
+    foort_result* out;
+    uint64_t n;
+    const ImageConst* images;
+    uint32_t n_images;
+    uint32_t pad;
+    unsigned long long* ctr;          // kNumCtr counters
+    const volatile int32_t* cancel;   // host flag in mapped pinned memory (may be null)
+    unsigned long long budget;        // 0 = unlimited
+};
+
+}  // namespace foort

@@ -1,0 +1,13 @@
+// FP64 kernel instantiations for metric kMankoNovikov.
+#include "kernel_fp64.cuh"
+#include "kernels.h"
+
+namespace foort {
+
+const void* fp64_kernel_mn(int integrator) {
+    if (integrator == FOORT_INTEGRATOR_RK4)
+        return reinterpret_cast<const void*>(&integrate_fp64_kernel<kMankoNovikov, FOORT_INTEGRATOR_RK4>);
+    return reinterpret_cast<const void*>(&integrate_fp64_kernel<kMankoNovikov, FOORT_INTEGRATOR_VERLET>);
+}
+
+}  // namespace foort

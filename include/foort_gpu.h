@@ -94,6 +94,7 @@ typedef struct foort_image_desc {
     double cam_dir[4];       /* only {0,-1,0,0} is supported, as in the reference     */
     double screen_size[2];
     double screen_center[2];
+    double horizon_eps;      /* > 0: this image's Epsilon_Horizon, else the run's     */
 } foort_image_desc;
 
 /*
@@ -220,6 +221,19 @@ const char* foort_gpu_last_error(const foort_ctx* ctx);
 /* Horizon radius the reference gives the metric (Metric.cpp:113, 250, 385, 496);
  * 0 for flat space. */
 double foort_horizon_radius(int32_t metric_id, const double* metric_params);
+
+/* 1 if this build has a kernel for (metric, integrator, precision), else 0. The
+ * reference selects these at run time through Config::GetMetric / GetGeodesicIntegrator
+ * (Config.cpp:123-323, 985-1071). */
+int foort_gpu_has_kernel(int32_t metric_id, int32_t integrator_id, int32_t precision);
+
+/* sizeof() of the ABI structs, for binding checks: 0 foort_pixel, 1 foort_result,
+ * 2 foort_run_desc, 3 foort_image_desc, 4 foort_stats; 0 otherwise. Engine extension. */
+uint64_t foort_abi_size(int32_t which);
+
+/* Measured FP32 and FP64 FMA throughput of the current GPU in TFLOP/s (an FMA counts as
+ * two operations): the denominators of the engine's ALU roofline. Engine extension. */
+int foort_measure_peaks(double* fp32_tflops, double* fp64_tflops);
 
 #ifdef __cplusplus
 }

@@ -589,13 +589,15 @@ int check_terms(const Opts& o, Lane& L) {
     return FOORT_TERMCODE_CONTINUE;
 }
 
-Opts make_opts(const foort_run_desc& d, const MetricDef& m) {
+Opts make_opts(const foort_run_desc& d, const MetricDef& m, const foort_image_desc& im) {
     Opts o{};
     o.term_flags = d.term_flags;
     // Config.cpp:644-683: Horizon only exists for metrics with a horizon.
     if (d.metric_id == FOORT_METRIC_FLAT) o.term_flags &= ~FOORT_TERM_HORIZON;
     o.diag_flags = d.diag_flags;
-    o.h_eps = d.horizon_eps; o.rh = m.rh; o.h_every = d.horizon_every;
+    o.h_eps = im.horizon_eps > 0.0 ? im.horizon_eps : d.horizon_eps;
+    o.rh = m.rh;
+    o.h_every = d.horizon_every;
     o.b_rad = d.boundary_radius; o.b_every = d.boundary_every;
     o.t_max = d.timeout_max_steps; o.t_every = d.timeout_every;
     o.th_eps = d.theta_eps; o.th_every = d.theta_every;
@@ -670,7 +672,7 @@ int run(const foort_run_desc* d, const foort_pixel* px, uint64_t n, real du0, re
         ms[i] = make_metric(d->metric_id, d->images[i].metric_params, d->rlog != 0);
         if (d->metric_id == FOORT_METRIC_FLAT) ms[i].rlog = false;
         cs[i] = make_camera(ms[i], d->images[i]);
-        os[i] = make_opts(*d, ms[i]);
+        os[i] = make_opts(*d, ms[i], d->images[i]);
     }
     for (uint64_t i = 0; i < n; ++i)
         if (px[i].image >= d->n_images) return FOORT_E_BADARG;

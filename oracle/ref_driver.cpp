@@ -74,14 +74,14 @@ std::unique_ptr<Metric> make_metric(const foort_run_desc* d, const double* p) {
 }
 
 // Set the process-global options the way Config.cpp:393-1071 would for these settings.
-GeodesicIntegratorFunc set_globals(const foort_run_desc* d, const Metric* M, TermBitflag& terms) {
+GeodesicIntegratorFunc set_globals(const foort_run_desc* d, const Metric* M, TermBitflag& terms, double heps) {
     SetOutputLevel(OutputLevel::Level_0_WARNING);
     const SphericalHorizonMetric* sm = dynamic_cast<const SphericalHorizonMetric*>(M);
     bool rl = sm && sm->getrLogScale();
     terms = static_cast<TermBitflag>(d->term_flags);
     if (terms & Term_Horizon) {
         if (!sm) terms &= static_cast<TermBitflag>(~Term_Horizon);
-        else HorizonTermination::TermOptions.reset(new HorizonTermOptions{sm->getHorizonRadius(), rl, d->horizon_eps, d->horizon_every});
+        else HorizonTermination::TermOptions.reset(new HorizonTermOptions{sm->getHorizonRadius(), rl, heps, d->horizon_every});
     }
     BoundarySphereTermination::TermOptions.reset(new BoundarySphereTermOptions{d->boundary_radius, rl, d->boundary_every});
     TimeOutTermination::TermOptions.reset(new TimeOutTermOptions{d->timeout_max_steps, d->timeout_every});
@@ -159,7 +159,7 @@ int ref_integrate(const foort_run_desc* d, const foort_pixel* px, uint64_t n, fo
         std::unique_ptr<Metric> M = make_metric(d, I.metric_params);
         std::unique_ptr<Source> S(new NoSource(M.get()));
         TermBitflag terms;
-        GeodesicIntegratorFunc integ = set_globals(d, M.get(), terms);
+        GeodesicIntegratorFunc integ = set_globals(d, M.get(), terms, I.horizon_eps > 0.0 ? I.horizon_eps : d->horizon_eps);
         DiagBitflag diags = static_cast<DiagBitflag>(d->diag_flags), vd = static_cast<DiagBitflag>(d->value_diag);
         ViewScreen view(Point{I.cam_pos[0], I.cam_pos[1], I.cam_pos[2], I.cam_pos[3]},
                         OneIndex{I.cam_dir[0], I.cam_dir[1], I.cam_dir[2], I.cam_dir[3]},
@@ -221,7 +221,7 @@ int ref_run(const foort_run_desc* d, const ref_mesh_spec* ms, const char* prefix
     std::unique_ptr<Metric> M = make_metric(d, I.metric_params);
     std::unique_ptr<Source> S(new NoSource(M.get()));
     TermBitflag terms;
-    GeodesicIntegratorFunc integ = set_globals(d, M.get(), terms);
+    GeodesicIntegratorFunc integ = set_globals(d, M.get(), terms, I.horizon_eps > 0.0 ? I.horizon_eps : d->horizon_eps);
     DiagBitflag diags = static_cast<DiagBitflag>(d->diag_flags), vd = static_cast<DiagBitflag>(d->value_diag);
     std::unique_ptr<ViewScreen> view(new ViewScreen(
         Point{I.cam_pos[0], I.cam_pos[1], I.cam_pos[2], I.cam_pos[3]}, OneIndex{I.cam_dir[0], I.cam_dir[1], I.cam_dir[2], I.cam_dir[3]},
@@ -271,7 +271,7 @@ int ref_first_line(const foort_run_desc* d, const ref_mesh_spec* ms, char* buf, 
     std::unique_ptr<Metric> M = make_metric(d, I.metric_params);
     std::unique_ptr<Source> S(new NoSource(M.get()));
     TermBitflag terms;
-    set_globals(d, M.get(), terms);
+    set_globals(d, M.get(), terms, I.horizon_eps > 0.0 ? I.horizon_eps : d->horizon_eps);
     DiagBitflag diags = static_cast<DiagBitflag>(d->diag_flags), vd = static_cast<DiagBitflag>(d->value_diag);
     ViewScreen view(Point{I.cam_pos[0], I.cam_pos[1], I.cam_pos[2], I.cam_pos[3]},
                     OneIndex{I.cam_dir[0], I.cam_dir[1], I.cam_dir[2], I.cam_dir[3]},
