@@ -29,6 +29,9 @@ INTEGRATOR_VERLET = 1
 PREC_FP64 = 0
 PREC_MIXED = 1
 
+MIXED_FF_DECISIONS = 0x1
+MIXED_FP64_NEAR_HORIZON = 0x2
+
 # TermBitflag (Terminations.h:29-33)
 TERM_BOUNDARY_SPHERE = 0x1
 TERM_TIMEOUT = 0x2
@@ -53,6 +56,7 @@ ERR_VERLET_ITER = 0x2
 ERR_BUDGET = 0x4
 ERR_CANCELLED = 0x8
 ERR_UNFINISHED = 0x10
+ERR_BADPIXEL = 0x20
 
 
 class UpdateFreq(C.Structure):
@@ -83,7 +87,7 @@ class RunDesc(C.Structure):
         ("term_flags", C.c_uint32),
         ("diag_flags", C.c_uint32),
         ("value_diag", C.c_uint32),
-        ("reserved0", C.c_uint32),
+        ("mixed_options", C.c_uint32),
         ("horizon_eps", C.c_double),
         ("horizon_every", C.c_uint64),
         ("boundary_radius", C.c_double),
@@ -97,6 +101,7 @@ class RunDesc(C.Structure):
         ("closest_freq", UpdateFreq),
         ("geopos_freq", UpdateFreq),
         ("geopos_output_steps", C.c_uint64),
+        ("mixed_fp64_margin", C.c_double),
         ("n_images", C.c_uint32),
         ("reserved1", C.c_uint32),
         ("images", C.POINTER(ImageDesc)),

@@ -41,9 +41,15 @@ def _stale(obj, src, newest_header):
     return t < os.path.getmtime(src) or t < newest_header
 
 
+# The mixed-precision kernels use FP32 division / square root with 2-ulp accuracy and
+# flush FP32 denormals; their FP64 code is unaffected.
+MIXED_FLAGS = ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
+
+
 def _compile(src, obj, extra, verbose):
     if src.endswith(".cu"):
-        cmd = [nvcc()] + NVFLAGS + extra + ["-c", src, "-o", obj]
+        more = MIXED_FLAGS if os.path.basename(src).startswith("k_mixed_") else []
+        cmd = [nvcc()] + NVFLAGS + more + extra + ["-c", src, "-o", obj]
     else:
         cmd = ["g++"] + CXXFLAGS + ["-I" + os.path.join(HERE, "..", "include"), "-I/usr/local/cuda/include",
                                     "-c", src, "-o", obj]

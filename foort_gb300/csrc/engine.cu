@@ -189,12 +189,15 @@ RunConst make_run_const(const foort_run_desc& d) {
     R.cr_finish = d.closest_freq.at_finish;
     R.verlet_cap = 1000;
     R.poll_steps = 512;
+    R.mixed_options = d.mixed_options;
+    R.mixed_fp64_margin = (d.mixed_options & FOORT_MIXED_FP64_NEAR_HORIZON) ? d.mixed_fp64_margin : 0.0;
     return R;
 }
 
 const void* select_kernel(const RunConst& R) {
-    return R.precision == FOORT_PREC_MIXED ? mixed_kernel(R.metric_id, R.integrator)
-                                           : fp64_kernel(R.metric_id, R.integrator);
+    if (R.precision == FOORT_PREC_MIXED)
+        return mixed_kernel_variant(R.metric_id, R.integrator, !(R.mixed_options & FOORT_MIXED_FF_DECISIONS));
+    return fp64_kernel(R.metric_id, R.integrator);
 }
 
 int ensure_capacity(foort_ctx* ctx, uint64_t n) {

@@ -11,6 +11,25 @@ namespace foort {
 // Truncated pi of the reference (Geometry.h:44); every angular test uses it.
 constexpr double kRefPi = 3.1415926535;
 
+// Constants of the mixed-precision kernel (per image). Pairs [2] are float-float
+// (hi, lo) splits of a double; thresholds are in ln r in log-r mode.
+struct MixedConst {
+    float q[6];        // metric constants in FP32
+    float rp[2];       // r_+ (Delta = (r - r_+)(r - r_-))
+    float rm[2];       // r_-
+    float lrp[2];      // ln r_+
+    float lrm[2];      // ln r_- (unused when r_- = 0)
+    double rpv, rmv;   // r_+, r_- as doubles
+    float r_fp64;      // lanes with x1 below this use the FP64 right-hand side (0: never)
+    float hthr[2];     // Horizon: r_h (1 + eps)
+    float hthr0[2];    // Horizon with r_h = 0: eps
+    float bthr[2];     // BoundarySphere radius
+    float theps[2];    // ThetaSingularity epsilon
+    float pi[2];       // the reference's pi
+    float mpio2[2];    // -pi / 2
+    float eqthr[2];    // EquatorialPasses threshold: pi / 2 * Threshold
+};
+
 // Per-image constants, computed once on the host (ViewScreen.cpp:10-73).
 struct ImageConst {
     MetricConst m;
@@ -22,11 +41,7 @@ struct ImageConst {
     double size[2];     // screen size
     double center[2];   // screen center
     double h_eps;       // Epsilon_Horizon of this image (relative)
-    // Mixed-precision kernel: FP32 copies of the metric constants and the radius below
-    // which a lane evaluates its right-hand side in FP64.
-    float qf[6];
-    float rhf;
-    double r_fp64;
+    MixedConst mx;
 };
 
 // Run options (process globals in the reference, Config.cpp:11-28 and
@@ -52,6 +67,9 @@ struct RunConst {
     int32_t cr_start, cr_finish;
     int32_t verlet_cap;   // cap on Verlet velocity iterations (the reference has none)
     int32_t poll_steps;   // steps between budget / cancel polls
+    uint32_t mixed_options;
+    uint32_t pad0;
+    double mixed_fp64_margin;
 };
 
 // Scratch counters of one launch (device memory, zeroed before each launch).

@@ -195,8 +195,8 @@ __device__ __forceinline__ bool finite4(const double a[4]) {
 //   struct Lane;                       lane state
 //   init(L, I, R, px)                  Geodesic::Reset with the pixel's initial conditions
 //   step(L, I, R) -> bool              one Geodesic::Update; true while the lane runs
-//   finish(L, out)                     write the lane's record
-//   stop(L, out, err)                  write a partial record (budget / cancel)
+//   finish(L, R, out)                  write the lane's record
+//   stop(L, R, out, err)               write a partial record (budget / cancel)
 //   counters: L.rhs, L.fp64            accumulated per lane, flushed at each poll
 //
 // Every warp takes pixels from one global counter (one atomic per warp, shared by the
@@ -233,11 +233,13 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                 if (!active) {
                     const uint64_t my = base + __popc(need & lt_mask);
                     if (my < A.n) {
+                        const foort_pixel p = A.px[my];
                         if (stopping) {
                             write_unstarted(&A.out[my], stop_err);
+                        } else if (p.image >= A.n_images || p.grid < 2) {
+                            write_unstarted(&A.out[my], FOORT_ERR_BADPIXEL);
                         } else {
                             idx = my;
-                            const foort_pixel p = A.px[my];
                             E::init(L, A.images[p.image], R, p);
                             active = true;
                         }
@@ -255,7 +257,7 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                 const ImageConst& I = A.images[L.img];
                 ++lane_steps;
                 if (!E::step(L, I, R)) {
-                    E::finish(L, &A.out[idx]);
+                    E::finish(L, R, &A.out[idx]);
                     active = false;
                     ++lane_done;
                 }
@@ -292,7 +294,7 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                 stopping = true;
                 stop_err = (st & kStatusCancelled) ? FOORT_ERR_CANCELLED : FOORT_ERR_BUDGET;
                 if (active) {
-                    E::stop(L, &A.out[idx], stop_err);
+                    E::stop(L, R, &A.out[idx], stop_err);
                     active = false;
                 }
             }

@@ -159,10 +159,10 @@ struct Fp64Engine {
         return L.term == FOORT_TERMCODE_CONTINUE;
     }
 
-    static __device__ __forceinline__ void finish(const Lane& L, foort_result* o) {
+    static __device__ __forceinline__ void finish(const Lane& L, const RunConst&, foort_result* o) {
         write_result(o, L.term, L.err, L.steps, L.lam, L.x, L.v, L.D);
     }
-    static __device__ __forceinline__ void stop(const Lane& L, foort_result* o, uint32_t err) {
+    static __device__ __forceinline__ void stop(const Lane& L, const RunConst&, foort_result* o, uint32_t err) {
         write_result(o, FOORT_TERMCODE_CONTINUE, L.err | err, L.steps, L.lam, L.x, L.v, L.D);
     }
 };

@@ -1,0 +1,435 @@
+// Mixed-precision integration kernel: FP32 bulk, compensated state.
+//
+// Per lane the state (t, r, theta, phi), the 4-velocity and the affine parameter are
+// float-float pairs (hi + lo, ~48 significant bits), updated each step with error-free
+// transformations (Knuth's TwoSum, FMA-based TwoProd), so that rounding does not
+// accumulate over the 10^4-10^5 steps of a geodesic. The right-hand side runs in FP32:
+// analytic metric derivatives (gen_christoffel.inc) combined in Lagrangian form,
+//     a^mu = -1/2 g^{mu s} (2 u^n d_n g_{s p} u^p - d_s g_{n p} u^n u^p),
+// which needs only d_r g_ij and d_theta g_ij of the five non-zero components. The
+// near-horizon factor Delta = (r - r_+)(r - r_-) is formed from the compensated radius.
+//
+// Decisions (terminations, equator crossings, closest radius) are taken on the
+// compensated state; with DECIDE64 they are taken in FP64 on its exact double value,
+// as the reference takes them, otherwise by float-float comparisons that agree with
+// the FP64 ones except within 2^-48 (relative) of a threshold. Optionally, lanes closer
+// than I.r_fp64 to the horizon evaluate their right-hand side in FP64.
+#pragma once
+
+#include "gen_christoffel.inc"
+#include "kernel_common.cuh"
+
+namespace foort {
+
+// ---- float-float arithmetic --------------------------------------------------------
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+    ff s = two_sum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    ff s = two_sum(a.hi, b.hi);
+    ff t = two_sum(a.lo, b.lo);
+    s.lo = __fadd_rn(s.lo, t.hi);
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo = __fadd_rn(s.lo, t.lo);
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.hi, -a.lo}; }
+// exact product of two floats as a float-float (FMA-based TwoProd)
+__device__ __forceinline__ ff two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool ff_neg_sign(ff a) { return a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f); }
+__device__ __forceinline__ ff ff_abs(ff a) { return ff_neg_sign(a) ? ff_neg(a) : a; }
+__device__ __forceinline__ double ff_d(ff a) { return static_cast<double>(a.hi) + static_cast<double>(a.lo); }
+__device__ __forceinline__ float ff_f(ff a) { return a.hi + a.lo; }
+__host__ __device__ inline void ff_split(double d, float& hi, float& lo) {
+    hi = static_cast<float>(d);
+    lo = static_cast<float>(d - static_cast<double>(hi));
+}
+__device__ __forceinline__ ff ff_of(const float* p) { return {p[0], p[1]}; }
+
+// ---- metric plugins in analytic form -------------------------------------------------
+template <typename T>
+struct G5T {
+    T tt, tp, rr, hh, pp;
+};
+
+template <int MID>
+struct MixedMetric;
+
+// kInline: small bodies are inlined into each of the RK4 stages; large ones (Johannsen,
+// ~300 temporaries) are called, which keeps them out of the register allocation of
+// the stepping loop.
+#define FOORT_DEFINE_MIXED_METRIC(ID, BODY, INL)                                                     \
+    template <>                                                                                      \
+    struct MixedMetric<ID> {                                                                         \
+        static constexpr bool kInline = INL;                                                         \
+        template <typename T>                                                                        \
+        static __device__ __forceinline__ void eval(const T* q, T r, T dp, T dm, T s, T c, G5T<T>& dr, \
+                                                    G5T<T>& dh, G5T<T>& gu, T& grr) {                \
+            (void)q; (void)dp; (void)dm;                                                             \
+            BODY                                                                                     \
+        }                                                                                            \
+    };
+
+FOORT_DEFINE_MIXED_METRIC(kKerr, FOORT_MIXED_BODY_KERR, true)
+FOORT_DEFINE_MIXED_METRIC(kJohannsen, FOORT_MIXED_BODY_JOHANNSEN, false)
+FOORT_DEFINE_MIXED_METRIC(kFlat, FOORT_MIXED_BODY_FLAT, true)
+
+// a^mu from d_1 g, d_2 g (derivatives in the integration coordinates x1, x2), g^uu, u.
+template <typename T>
+__device__ __forceinline__ void accel_lagrange(const G5T<T>& d1, const G5T<T>& d2, const G5T<T>& gu, const T u[4],
+                                               T a[4]) {
+    const T w1t = d1.tt * u[0] + d1.tp * u[3], w1r = d1.rr * u[1], w1h = d1.hh * u[2], w1p = d1.tp * u[0] + d1.pp * u[3];
+    const T w2t = d2.tt * u[0] + d2.tp * u[3], w2r = d2.rr * u[1], w2h = d2.hh * u[2], w2p = d2.tp * u[0] + d2.pp * u[3];
+    const T q1 = u[0] * w1t + u[1] * w1r + u[2] * w1h + u[3] * w1p;
+    const T q2 = u[0] * w2t + u[1] * w2r + u[2] * w2h + u[3] * w2p;
+    const T Ft = T(2) * (u[1] * w1t + u[2] * w2t);
+    const T Fp = T(2) * (u[1] * w1p + u[2] * w2p);
+    const T Fr = T(2) * (u[1] * w1r + u[2] * w2r) - q1;
+    const T Fh = T(2) * (u[1] * w1h + u[2] * w2h) - q2;
+    a[0] = T(-0.5) * (gu.tt * Ft + gu.tp * Fp);
+    a[3] = T(-0.5) * (gu.tp * Ft + gu.pp * Fp);
+    a[1] = T(-0.5) * gu.rr * Fr;
+    a[2] = T(-0.5) * gu.hh * Fh;
+}
+
+// Right-hand side at (x1, theta) with velocity u. `x1` is the compensated radial
+// coordinate (r, or ln r in log-r mode); r_+ / r_- (and their logarithms) come from the
+// image constants so that dp = r - r_+ and dm = r - r_- are accurate near the horizon.
+template <int MID, typename T>
+__device__ __forceinline__ void rhs_analytic(const T* q, const MixedConst& mc, bool rlog, ff x1, T th, const T u[4],
+                                             T a[4]) {
+    T r, dp, dm;
+    if (!rlog) {
+        r = T(x1.hi) + T(x1.lo);
+        dp = T(__fsub_rn(x1.hi, mc.rp[0])) + (T(x1.lo) - T(mc.rp[1]));
+        dm = T(__fsub_rn(x1.hi, mc.rm[0])) + (T(x1.lo) - T(mc.rm[1]));
+    } else {
+        const T u1 = T(x1.hi) + T(x1.lo);
+        r = exp(u1);
+        dp = T(mc.rpv) * expm1((T(x1.hi) - T(mc.lrp[0])) + (T(x1.lo) - T(mc.lrp[1])));
+        dm = (mc.rmv > 0.0) ? T(mc.rmv) * expm1((T(x1.hi) - T(mc.lrm[0])) + (T(x1.lo) - T(mc.lrm[1]))) : r;
+    }
+    T s, c;
+    sincos(th, &s, &c);
+    G5T<T> dr, dh, gu;
+    T grr;
+    MixedMetric<MID>::template eval<T>(q, r, dp, dm, s, c, dr, dh, gu, grr);
+    if (rlog) {
+        // x1 = ln r: d_x1 = r d_r, g_11 = r^2 g_rr, g^11 = g^rr / r^2
+        const T r2 = r * r;
+        dr.tt *= r; dr.tp *= r; dr.hh *= r; dr.pp *= r;
+        dr.rr = r * (T(2) * r * grr + r2 * dr.rr);
+        dh.rr *= r2;
+        gu.rr /= r2;
+    }
+    accel_lagrange(dr, dh, gu, u, a);
+}
+
+template <int MID>
+__device__ __noinline__ void rhs_f32_called(const float* q, const MixedConst& mc, bool rlog, ff x1, float th,
+                                            const float u[4], float a[4]) {
+    rhs_analytic<MID, float>(q, mc, rlog, x1, th, u, a);
+}
+
+template <int MID>
+__device__ __noinline__ void rhs_fp64_path(const double* q, const MixedConst& mc, bool rlog, ff x1, double th,
+                                           const float uf[4], float a[4]) {
+    double u[4] = {uf[0], uf[1], uf[2], uf[3]}, ad[4];
+    rhs_analytic<MID, double>(q, mc, rlog, x1, th, u, ad);
+    for (int i = 0; i < 4; ++i) a[i] = static_cast<float>(ad[i]);
+}
+
+// Integrators::GetAdaptiveStep (Integrators.cpp:34-46) in FP32.
+__device__ __forceinline__ float adaptive_step_f32(const RunConst& R, float th, const float v[4]) {
+    const float eps = static_cast<float>(R.eps);
+    const float pi = static_cast<float>(kRefPi);
+    const float d1 = eps / (fabsf(v[1]) + 1e-20f);
+    const float m = (pi - th < th) ? pi - th : th;
+    const float d2 = eps * m / (fabsf(v[2]) + 1e-20f);
+    const float d3 = eps / fabsf(v[3] + 1e-20f);
+    const float h = 1.f / (1.f / fabsf(d1) + 1.f / fabsf(d2) + 1.f / fabsf(d3));
+    const float hmin = static_cast<float>(R.hmin);
+    return (h < hmin) ? hmin : h;
+}
+
+template <int MID, int INTEG, bool DECIDE64>
+struct MixedEngine {
+    struct Lane {
+        ff x[4], v[4];
+        ff lam;
+        uint64_t steps;
+        TermState T;
+        // diagnostics on the compensated state
+        int32_t quad, passes;
+        uint64_t cE, cC;
+        ff prev;      // previous theta sample (hi = -1: none yet)
+        ff rmin;      // closest radius so far; ln r in log-r mode
+        bool has_rmin;
+        uint32_t err = 0;
+        uint32_t img = 0;
+        uint32_t rhs = 0;
+        uint32_t fp64 = 0;
+        int32_t term = 0;
+    };
+
+    static __device__ __forceinline__ void load_double(const Lane& L, double x[4], double v[4]) {
+        for (int i = 0; i < 4; ++i) {
+            x[i] = ff_d(L.x[i]);
+            v[i] = ff_d(L.v[i]);
+        }
+    }
+
+    static __device__ __forceinline__ void init(Lane& L, const ImageConst& I, const RunConst& R, const foort_pixel& p) {
+        double x[4], v[4];
+        initial_conditions(I, p, x, v);
+        for (int i = 0; i < 4; ++i) {
+            ff_split(x[i], L.x[i].hi, L.x[i].lo);
+            ff_split(v[i], L.v[i].hi, L.v[i].lo);
+        }
+        L.lam = {0.f, 0.f};
+        L.steps = 0;
+        L.err = 0;
+        L.term = FOORT_TERMCODE_CONTINUE;
+        L.img = p.image;
+        L.quad = 0;
+        L.passes = 0;
+        L.cE = 0;
+        L.cC = 0;
+        L.prev = {-1.f, 0.f};
+        L.rmin = {-1.f, 0.f};
+        L.has_rmin = false;
+        L.T.cH = L.T.cB = L.T.cT = L.T.cTh = 0;
+        L.T.tcur = 0;
+        diags(L, I, R, true);  // Geodesic::Reset's start sample at lambda = 0
+    }
+
+    // EquatorialPasses and ClosestRadius updates (Diagnostics.cpp:351-380, :427-446) on
+    // the compensated state; FourColorScreen at termination (Diagnostics.cpp:159-200).
+    static __device__ __forceinline__ void diags(Lane& L, const ImageConst& I, const RunConst& R, bool at_start) {
+        const double lamd = at_start ? 0.0 : 1.0;  // only compared with 0 by DecideUpdate
+        if (R.diag_flags & FOORT_DIAG_FOUR_COLOR_SCREEN) {
+            if (L.term == FOORT_TERMCODE_BOUNDARY_SPHERE) L.quad = four_color_quadrant(ff_d(L.x[2]), ff_d(L.x[3]));
+        }
+        if (R.diag_flags & FOORT_DIAG_EQUATORIAL_PASSES) {
+            if (diag_decide(R.eq_every, R.eq_start, R.eq_finish, L.cE, lamd, L.term)) {
+                if (DECIDE64) {
+                    const double th = ff_d(L.x[2]);
+                    if (fabs(th - kRefPi / 2.0) > kRefPi / 2.0 * R.eq_thr) {
+                        const double pv = ff_d(L.prev);
+                        if (pv > 0 && ((pv - kRefPi / 2.0) * (th - kRefPi / 2.0)) < 0.0) ++L.passes;
+                        L.prev = L.x[2];
+                    }
+                } else {
+                    const ff d = ff_add(L.x[2], ff_of(I.mx.mpio2));
+                    if (ff_lt(ff_of(I.mx.eqthr), ff_abs(d))) {
+                        if (L.prev.hi > 0.f) {
+                            const ff dprev = ff_add(L.prev, ff_of(I.mx.mpio2));
+                            if (ff_neg_sign(dprev) != ff_neg_sign(d)) ++L.passes;
+                        }
+                        L.prev = L.x[2];
+                    }
+                }
+            }
+            if (L.term == FOORT_TERMCODE_HORIZON) L.passes = -L.passes;
+        }
+        if (R.diag_flags & FOORT_DIAG_CLOSEST_RADIUS) {
+            if (diag_decide(R.cr_every, R.cr_start, R.cr_finish, L.cC, lamd, L.term)) {
+                // in log-r mode ln r is tracked (exp is monotonic) and exponentiated once
+                if (!L.has_rmin || ff_lt(L.x[1], L.rmin)) {
+                    L.rmin = L.x[1];
+                    L.has_rmin = true;
+                }
+            }
+        }
+    }
+
+    static __device__ __forceinline__ int terms(Lane& L, const ImageConst& I, const RunConst& R) {
+        if (DECIDE64) {
+            const double x1 = ff_d(L.x[1]);
+            const double r = R.rlog ? exp(x1) : x1;
+            return check_terms(R, I.m.rh, I.h_eps, r, ff_d(L.x[2]), L.T);
+        }
+        // Same order and cadence as check_terms; thresholds precomputed as float-float
+        // (in ln r in log-r mode).
+        if (R.term_flags & FOORT_TERM_HORIZON) {
+            if (term_decide(R.h_every, L.T.cH)) {
+                if (ff_lt(L.x[1], ff_of(I.mx.hthr)) || (I.m.rh == 0.0 && ff_lt(L.x[1], ff_of(I.mx.hthr0))))
+                    return FOORT_TERMCODE_HORIZON;
+            }
+        }
+        if (R.term_flags & FOORT_TERM_BOUNDARY_SPHERE) {
+            if (term_decide(R.b_every, L.T.cB)) {
+                if (ff_lt(ff_of(I.mx.bthr), L.x[1])) return FOORT_TERMCODE_BOUNDARY_SPHERE;
+            }
+        }
+        if (R.term_flags & FOORT_TERM_TIMEOUT) {
+            if (term_decide(R.t_every, L.T.cT)) {
+                if (L.T.tcur >= R.t_max) return FOORT_TERMCODE_TIMEOUT;
+                ++L.T.tcur;
+            }
+        }
+        if (R.term_flags & FOORT_TERM_THETA_SINGULARITY) {
+            if (term_decide(R.th_every, L.T.cTh)) {
+                const ff e = ff_of(I.mx.theps);
+                if (ff_lt(ff_abs(L.x[2]), e) || ff_lt(ff_abs(ff_add(ff_of(I.mx.pi), ff_neg(L.x[2]))), e))
+                    return FOORT_TERMCODE_THETA_SINGULARITY;
+            }
+        }
+        return FOORT_TERMCODE_CONTINUE;
+    }
+
+    static __device__ __forceinline__ void rhs(const ImageConst& I, const RunConst& R, Lane& L, ff x1, float th,
+                                               const float u[4], float a[4]) {
+        const bool rlog = R.rlog != 0;
+        if (I.mx.r_fp64 > 0.f && x1.hi < I.mx.r_fp64) {
+            rhs_fp64_path<MID>(I.m.q, I.mx, rlog, x1, static_cast<double>(th), u, a);
+            ++L.fp64;
+        } else if (MixedMetric<MID>::kInline) {
+            rhs_analytic<MID, float>(I.mx.q, I.mx, rlog, x1, th, u, a);
+        } else {
+            rhs_f32_called<MID>(I.mx.q, I.mx, rlog, x1, th, u, a);
+        }
+    }
+
+    static __device__ __forceinline__ bool step(Lane& L, const ImageConst& I, const RunConst& R) {
+        float uf[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) uf[i] = ff_f(L.v[i]);
+        const float th0 = ff_f(L.x[2]);
+        const float h = adaptive_step_f32(R, th0, uf);
+        float du[4];
+        float dxc[4];  // O(h^2) part of the position increment
+        if (INTEG == FOORT_INTEGRATOR_RK4) {
+            float k1[4], k2[4], k3[4], k4[4], us[4];
+            const float hh = 0.5f * h;
+            rhs(I, R, L, L.x[1], th0, uf, k1);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
+            rhs(I, R, L, ff_add_f(L.x[1], hh * uf[1]), th0 + hh * uf[2], us, k2);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
+            rhs(I, R, L, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])), th0 + hh * (uf[2] + hh * k1[2]), us, k3);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
+            rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), th0 + h * (uf[2] + hh * k2[2]), us, k4);
+            const float h6 = h * (1.f / 6.f), hh6 = h * h6;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                du[i] = h6 * (k1[i] + 2.f * k2[i] + 2.f * k3[i] + k4[i]);
+                dxc[i] = hh6 * (k1[i] + k2[i] + k3[i]);
+            }
+            L.rhs += 4;
+        } else {
+            // velocity Verlet (Integrators.cpp:99-152); the velocity change of each
+            // iteration is formed as h/2 (a1_new - a1_old), free of cancellation.
+            float a0[4], a1[4], vi[4];
+            rhs(I, R, L, L.x[1], th0, uf, a0);
+            const float hh2 = 0.5f * h * h;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                dxc[i] = hh2 * a0[i];
+                vi[i] = uf[i] + h * a0[i];
+            }
+            const ff x1n = ff_add_f(ff_add(L.x[1], two_prod(h, L.v[1].hi)), __fmaf_rn(h, L.v[1].lo, dxc[1]));
+            const float thn = th0 + h * uf[2] + dxc[2];
+            rhs(I, R, L, x1n, thn, vi, a1);
+            L.rhs += 2;
+            const float h2 = 0.5f * h;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) du[i] = h2 * (a0[i] + a1[i]);
+            if (R.vtol > 0.0) {
+                const float tol2 = static_cast<float>(R.vtol * R.vtol);
+                // first correction: nv - vi = h/2 (a1 - a0)
+                float dv[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) dv[i] = h2 * (a1[i] - a0[i]);
+                for (int it = 0;; ++it) {
+                    float num = 0.f, den = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float nvi = uf[i] + du[i];
+                        num += dv[i] * dv[i];
+                        den += nvi * nvi;
+                    }
+                    if (!(num / den > tol2)) break;
+                    if (it >= R.verlet_cap) {
+                        L.err |= FOORT_ERR_VERLET_ITER;
+                        break;
+                    }
+                    float a1n[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) vi[i] = uf[i] + du[i];
+                    rhs(I, R, L, x1n, thn, vi, a1n);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        dv[i] = h2 * (a1n[i] - a1[i]);
+                        a1[i] = a1n[i];
+                        du[i] = h2 * (a0[i] + a1[i]);
+                    }
+                    L.rhs += 1;
+                }
+            }
+        }
+        // x += h u + dxc;  u += du;  lambda += h  (compensated)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            ff hu = two_prod(h, L.v[i].hi);
+            hu.lo = __fmaf_rn(h, L.v[i].lo, hu.lo) + dxc[i];
+            L.x[i] = ff_add(L.x[i], hu);
+            L.v[i] = ff_add_f(L.v[i], du[i]);
+        }
+        L.lam = ff_add_f(L.lam, h);
+        ++L.steps;
+        L.term = terms(L, I, R);
+        diags(L, I, R, false);
+        if (!(isfinite(L.x[1].hi) && isfinite(L.x[2].hi) && isfinite(L.v[1].hi) && isfinite(L.v[2].hi) &&
+              isfinite(L.x[0].hi) && isfinite(L.x[3].hi) && isfinite(L.v[0].hi) && isfinite(L.v[3].hi))) {
+            L.err |= FOORT_ERR_NONFINITE;
+            if (L.term == FOORT_TERMCODE_CONTINUE && !(R.term_flags & FOORT_TERM_TIMEOUT)) return false;
+        }
+        return L.term == FOORT_TERMCODE_CONTINUE;
+    }
+
+    static __device__ __forceinline__ void write(const Lane& L, const RunConst& R, foort_result* o, int term,
+                                                 uint32_t err) {
+        double x[4], v[4];
+        load_double(L, x, v);
+        DiagState D;
+        D.quad = L.quad;
+        D.passes = L.passes;
+        double rm = -1.0;
+        if (L.has_rmin) rm = R.rlog ? exp(ff_d(L.rmin)) : ff_d(L.rmin);
+        if ((R.diag_flags & FOORT_DIAG_CLOSEST_RADIUS) && term == FOORT_TERMCODE_HORIZON) rm = 0.0;
+        D.rmin = rm;
+        write_result(o, term, err, L.steps, ff_d(L.lam), x, v, D);
+    }
+
+    static __device__ __forceinline__ void finish(const Lane& L, const RunConst& R, foort_result* o) {
+        write(L, R, o, L.term, L.err);
+    }
+    static __device__ __forceinline__ void stop(const Lane& L, const RunConst& R, foort_result* o, uint32_t err) {
+        write(L, R, o, FOORT_TERMCODE_CONTINUE, L.err | err);
+    }
+};
+
+}  // namespace foort

@@ -1,9 +1,54 @@
-// Mixed-precision kernels (placeholder until the FP32 plugins land).
+// Host side of the mixed-precision kernels: kernel registry and per-image constants.
+#include <cmath>
+
+#include "kernel_mixed.cuh"
 #include "kernels.h"
 
 namespace foort {
 
-const void* mixed_kernel(int, int) { return nullptr; }
-void fill_mixed_constants(int, ImageConst&, const RunConst&) {}
+const void* mixed_kernel_kerr(int integrator, bool decide64);
+const void* mixed_kernel_joh(int integrator, bool decide64);
+const void* mixed_kernel_flat(int integrator, bool decide64);
+
+// Mixed kernels exist for the metrics with analytic derivatives (gen_christoffel.py);
+// Rasheed-Larsen and Manko-Novikov run in FP64 only.
+const void* mixed_kernel_variant(int metric_id, int integ, bool decide64) {
+    switch (metric_id) {
+    case kKerr: return mixed_kernel_kerr(integ, decide64);
+    case kJohannsen: return mixed_kernel_joh(integ, decide64);
+    case kFlat: return mixed_kernel_flat(integ, decide64);
+    default: return nullptr;
+    }
+}
+
+const void* mixed_kernel(int metric_id, int integ) { return mixed_kernel_variant(metric_id, integ, true); }
+
+void fill_mixed_constants(int metric_id, ImageConst& ic, const RunConst& rc) {
+    MixedConst& mx = ic.mx;
+    for (int i = 0; i < 6; ++i) mx.q[i] = static_cast<float>(ic.m.q[i]);
+    double rp = 0.0, rm = 0.0;
+    if (metric_id == kKerr || metric_id == kJohannsen) {
+        const double a = ic.m.q[0];
+        rp = 1.0 + std::sqrt(1.0 - a * a);
+        rm = 1.0 - std::sqrt(1.0 - a * a);
+    }
+    mx.rpv = rp;
+    mx.rmv = rm;
+    ff_split(rp, mx.rp[0], mx.rp[1]);
+    ff_split(rm, mx.rm[0], mx.rm[1]);
+    ff_split(rp > 0 ? std::log(rp) : 0.0, mx.lrp[0], mx.lrp[1]);
+    ff_split(rm > 0 ? std::log(rm) : 0.0, mx.lrm[0], mx.lrm[1]);
+    const bool rlog = rc.rlog != 0;
+    auto coord = [rlog](double r) { return rlog ? std::log(r) : r; };
+    mx.r_fp64 = (rc.mixed_fp64_margin > 0.0 && rp > 0.0) ? static_cast<float>(coord(rp + rc.mixed_fp64_margin)) : 0.f;
+    const double rh = ic.m.rh;
+    ff_split(coord(rh * (1 + ic.h_eps)), mx.hthr[0], mx.hthr[1]);
+    ff_split(ic.h_eps > 0 ? coord(ic.h_eps) : (rlog ? -HUGE_VAL : 0.0), mx.hthr0[0], mx.hthr0[1]);
+    ff_split(coord(rc.b_rad), mx.bthr[0], mx.bthr[1]);
+    ff_split(rc.th_eps, mx.theps[0], mx.theps[1]);
+    ff_split(kRefPi, mx.pi[0], mx.pi[1]);
+    ff_split(-(kRefPi / 2.0), mx.mpio2[0], mx.mpio2[1]);
+    ff_split(kRefPi / 2.0 * rc.eq_thr, mx.eqthr[0], mx.eqthr[1]);
+}
 
 }  // namespace foort

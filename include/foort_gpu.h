@@ -54,6 +54,12 @@ extern "C" {
 #define FOORT_PREC_FP64 0  /* every operation in FP64, finite-difference Christoffels   */
 #define FOORT_PREC_MIXED 1 /* FP32 bulk with compensated state, FP64 where needed       */
 
+/* Options of the mixed-precision kernel (engine extension). By default its decisions
+ * (terminations, equator crossings, closest radius) are taken in FP64 on the exact
+ * double value of its compensated state. */
+#define FOORT_MIXED_FF_DECISIONS 0x1u      /* take them in float-float arithmetic instead */
+#define FOORT_MIXED_FP64_NEAR_HORIZON 0x2u /* FP64 right-hand side near the horizon       */
+
 /* TermBitflag, Terminations.h:29-33 */
 #define FOORT_TERM_BOUNDARY_SPHERE 0x1u
 #define FOORT_TERM_TIMEOUT 0x2u
@@ -79,6 +85,7 @@ extern "C" {
 #define FOORT_ERR_BUDGET 0x4u      /* stopped by the global step budget (term = 0)    */
 #define FOORT_ERR_CANCELLED 0x8u   /* stopped by foort_gpu_cancel (term = 0)          */
 #define FOORT_ERR_UNFINISHED 0x10u /* never started (launch stopped before it)        */
+#define FOORT_ERR_BADPIXEL 0x20u   /* image index out of range or grid < 2; skipped   */
 
 /* Diagnostic update cadence, Diagnostics.h:50-55 (UpdateFrequency). */
 typedef struct foort_update_freq {
@@ -115,7 +122,7 @@ typedef struct foort_run_desc {
     uint32_t term_flags;   /* FOORT_TERM_* bitflag                                    */
     uint32_t diag_flags;   /* FOORT_DIAG_* bitflag                                    */
     uint32_t value_diag;   /* the one diagnostic whose value feeds the Mesh           */
-    uint32_t reserved0;
+    uint32_t mixed_options; /* FOORT_MIXED_* bits (mixed precision only)             */
 
     double horizon_eps;          /* HorizonTermOptions::AtHorizonEps (relative)      */
     uint64_t horizon_every;      /* UpdateEveryNSteps                                 */
@@ -131,6 +138,9 @@ typedef struct foort_run_desc {
     foort_update_freq closest_freq;   /* ClosestRadiusOptions                         */
     foort_update_freq geopos_freq;    /* GeodesicPositionOptions                      */
     uint64_t geopos_output_steps;
+
+    double mixed_fp64_margin;        /* with FOORT_MIXED_FP64_NEAR_HORIZON: lanes with
+                                        r < r_+ + margin evaluate the RHS in FP64       */
 
     uint32_t n_images;               /* >= 1                                          */
     uint32_t reserved1;

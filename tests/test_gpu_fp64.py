@@ -27,7 +27,8 @@ FP64_P90_TOL = 1e-5
 @pytest.fixture(scope="module")
 def eng():
     import foort_gb300
-    foort_gb300.build.build()
+    from foort_gb300 import build as engine_build
+    engine_build.build()
     foort_gb300.check_layout()
     return foort_gb300
 
