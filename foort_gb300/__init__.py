@@ -53,6 +53,22 @@ def load():
     lib.foort_abi_size.restype = u64
     lib.foort_measure_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.foort_gpu_has_kernel.argtypes = [i32, i32, i32]
+    lib.foort_metric_christoffel.argtypes = [i32, vp, i32, vp, vp]
+    lib.foort_mesh_create_simple.argtypes = [u64, u32, u32, C.POINTER(vp)]
+    lib.foort_mesh_create_v2.argtypes = [u64, u64, i32, u64, i32, u32, u32, C.POINTER(vp)]
+    lib.foort_mesh_is_finished.argtypes = [vp]
+    lib.foort_mesh_cur_nr_geodesics.argtypes = [vp]
+    lib.foort_mesh_cur_nr_geodesics.restype = u64
+    lib.foort_mesh_grid.argtypes = [vp]
+    lib.foort_mesh_grid.restype = u64
+    lib.foort_mesh_rounds.argtypes = [vp]
+    lib.foort_mesh_rounds.restype = u64
+    lib.foort_mesh_get_pixels.argtypes = [vp, u32, vp]
+    lib.foort_mesh_geodesic_finished.argtypes = [vp, u64, vp, u32]
+    lib.foort_mesh_set_results.argtypes = [vp, vp, u64]
+    lib.foort_mesh_end_current_loop.argtypes = [vp]
+    lib.foort_mesh_destroy.argtypes = [vp]
+    lib.foort_mesh_destroy.restype = None
     _LIB = lib
     return lib
 
@@ -159,3 +175,72 @@ class Engine:
 def horizon_radius(metric_id, params):
     arr = (C.c_double * 6)(*([float(p) for p in params] + [0.0] * (6 - len(params))))
     return load().foort_horizon_radius(metric_id, C.cast(arr, C.c_void_p))
+
+
+class Mesh:
+    """A host mesh (include/foort_gpu.h foort_mesh_*): SimpleSquareMesh or
+    SquareSubdivisionMeshV2 with the reference's constructor arguments."""
+
+    def __init__(self, kind, diag_flags, value_diag, total_pixels=0, max_pixels=0, initial_pixels=0,
+                 max_subdivide=1, iteration_pixels=0, initial_sub_to_final=0):
+        self._lib = load()
+        self._m = C.c_void_p()
+        if kind == "simple":
+            rc = self._lib.foort_mesh_create_simple(total_pixels, diag_flags, value_diag, C.byref(self._m))
+        else:
+            rc = self._lib.foort_mesh_create_v2(max_pixels, initial_pixels, max_subdivide, iteration_pixels,
+                                                initial_sub_to_final, diag_flags, value_diag, C.byref(self._m))
+        if rc != 0:
+            raise FoortError(rc, "mesh creation failed")
+
+    @classmethod
+    def from_spec(cls, spec, diag_flags, value_diag):
+        kind, args = spec
+        if kind == "simple":
+            return cls("simple", diag_flags, value_diag, total_pixels=args * args)
+        return cls("v2", diag_flags, value_diag, **args)
+
+    def finished(self):
+        return bool(self._lib.foort_mesh_is_finished(self._m))
+
+    def size(self):
+        return self._lib.foort_mesh_cur_nr_geodesics(self._m)
+
+    def grid(self):
+        return self._lib.foort_mesh_grid(self._m)
+
+    def rounds(self):
+        return self._lib.foort_mesh_rounds(self._m)
+
+    def pixels(self, image=0, out=None):
+        n = self.size()
+        if out is None:
+            out = np.zeros(n, dtype=abi.PIXEL_DTYPE)
+        rc = self._lib.foort_mesh_get_pixels(self._m, image, out.ctypes.data)
+        if rc != 0:
+            raise FoortError(rc, "get_pixels failed")
+        return out[:n]
+
+    def set_values(self, values):
+        for i, v in enumerate(values):
+            arr = (C.c_double * 1)(float(v))
+            self._lib.foort_mesh_geodesic_finished(self._m, i, arr, 1)
+
+    def set_results(self, results):
+        rc = self._lib.foort_mesh_set_results(self._m, results.ctypes.data, len(results))
+        if rc != 0:
+            raise FoortError(rc, "set_results failed")
+
+    def end_round(self):
+        self._lib.foort_mesh_end_current_loop(self._m)
+
+    def close(self):
+        if self._m:
+            self._lib.foort_mesh_destroy(self._m)
+            self._m = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,80 @@
+// Analytic metric plugins (host + device), templated on the arithmetic type.
+//
+// Each plugin evaluates, at (r, theta), the derivatives d_r g_ij and d_theta g_ij of
+// the five non-zero covariant components, the contravariant components g^ij and g_rr
+// (gen_christoffel.inc, generated from the reference's Metric.cpp formulas). The
+// mixed-precision kernel runs them in FP32 (and in FP64 near the horizon when asked);
+// the host runs them in FP64 for foort_metric_christoffel().
+#pragma once
+
+#include <math.h>
+
+#include "gen_christoffel.inc"
+#include "metric_fp64.cuh"
+
+namespace foort {
+
+template <typename T>
+struct G5T {
+    T tt, tp, rr, hh, pp;
+};
+
+template <int MID>
+struct MixedMetric {
+    static constexpr bool kAvailable = false;
+    static constexpr bool kInline = true;
+};
+
+// kInline: small bodies are inlined into each of the RK4 stages; large ones (Johannsen,
+// ~300 temporaries) are called, which keeps them out of the register allocation of
+// the stepping loop.
+#define FOORT_DEFINE_MIXED_METRIC(ID, BODY, INL)                                                   \
+    template <>                                                                                    \
+    struct MixedMetric<ID> {                                                                       \
+        static constexpr bool kAvailable = true;                                                   \
+        static constexpr bool kInline = INL;                                                       \
+        template <typename T>                                                                      \
+        static FOORT_HD void eval(const T* q, T r, T dp, T dm, T s, T c, G5T<T>& dr, G5T<T>& dh,   \
+                                  G5T<T>& gu, T& grr) {                                            \
+            (void)q; (void)dp; (void)dm;                                                           \
+            BODY                                                                                   \
+        }                                                                                          \
+    };
+
+FOORT_DEFINE_MIXED_METRIC(kKerr, FOORT_MIXED_BODY_KERR, true)
+FOORT_DEFINE_MIXED_METRIC(kJohannsen, FOORT_MIXED_BODY_JOHANNSEN, false)
+FOORT_DEFINE_MIXED_METRIC(kFlat, FOORT_MIXED_BODY_FLAT, true)
+
+// d_x1 g and g^11 in log-r mode (x1 = ln r): d_x1 = r d_r, g_11 = r^2 g_rr,
+// g^11 = g^rr / r^2.
+template <typename T>
+FOORT_HD void to_log_r(T r, T grr, G5T<T>& dr, G5T<T>& dh, G5T<T>& gu) {
+    const T r2 = r * r;
+    dr.tt *= r;
+    dr.tp *= r;
+    dr.hh *= r;
+    dr.pp *= r;
+    dr.rr = r * (T(2) * r * grr + r2 * dr.rr);
+    dh.rr *= r2;
+    gu.rr /= r2;
+}
+
+// a^mu = -1/2 g^{mu s} (2 u^n d_n g_{s p} u^p - d_s g_{n p} u^n u^p), with d_1 g, d_2 g
+// the derivatives in the integration coordinates x1, x2.
+template <typename T>
+FOORT_HD void accel_lagrange(const G5T<T>& d1, const G5T<T>& d2, const G5T<T>& gu, const T u[4], T a[4]) {
+    const T w1t = d1.tt * u[0] + d1.tp * u[3], w1r = d1.rr * u[1], w1h = d1.hh * u[2], w1p = d1.tp * u[0] + d1.pp * u[3];
+    const T w2t = d2.tt * u[0] + d2.tp * u[3], w2r = d2.rr * u[1], w2h = d2.hh * u[2], w2p = d2.tp * u[0] + d2.pp * u[3];
+    const T q1 = u[0] * w1t + u[1] * w1r + u[2] * w1h + u[3] * w1p;
+    const T q2 = u[0] * w2t + u[1] * w2r + u[2] * w2h + u[3] * w2p;
+    const T Ft = T(2) * (u[1] * w1t + u[2] * w2t);
+    const T Fp = T(2) * (u[1] * w1p + u[2] * w2p);
+    const T Fr = T(2) * (u[1] * w1r + u[2] * w2r) - q1;
+    const T Fh = T(2) * (u[1] * w1h + u[2] * w2h) - q2;
+    a[0] = T(-0.5) * (gu.tt * Ft + gu.tp * Fp);
+    a[3] = T(-0.5) * (gu.tp * Ft + gu.pp * Fp);
+    a[1] = T(-0.5) * gu.rr * Fr;
+    a[2] = T(-0.5) * gu.hh * Fh;
+}
+
+}  // namespace foort

@@ -28,6 +28,8 @@ struct MixedConst {
     float pi[2];       // the reference's pi
     float mpio2[2];    // -pi / 2
     float eqthr[2];    // EquatorialPasses threshold: pi / 2 * Threshold
+    float eps[2];      // Integrators::epsilon
+    float hmin;        // Integrators::SmallestPossibleStepsize
 };
 
 // Per-image constants, computed once on the host (ViewScreen.cpp:10-73).

@@ -16,7 +16,7 @@
 // than I.r_fp64 to the horizon evaluate their right-hand side in FP64.
 #pragma once
 
-#include "gen_christoffel.inc"
+#include "analytic_metric.cuh"
 #include "kernel_common.cuh"
 
 namespace foort {
@@ -66,52 +66,6 @@ __host__ __device__ inline void ff_split(double d, float& hi, float& lo) {
 }
 __device__ __forceinline__ ff ff_of(const float* p) { return {p[0], p[1]}; }
 
-// ---- metric plugins in analytic form -------------------------------------------------
-template <typename T>
-struct G5T {
-    T tt, tp, rr, hh, pp;
-};
-
-template <int MID>
-struct MixedMetric;
-
-// kInline: small bodies are inlined into each of the RK4 stages; large ones (Johannsen,
-// ~300 temporaries) are called, which keeps them out of the register allocation of
-// the stepping loop.
-#define FOORT_DEFINE_MIXED_METRIC(ID, BODY, INL)                                                     \
-    template <>                                                                                      \
-    struct MixedMetric<ID> {                                                                         \
-        static constexpr bool kInline = INL;                                                         \
-        template <typename T>                                                                        \
-        static __device__ __forceinline__ void eval(const T* q, T r, T dp, T dm, T s, T c, G5T<T>& dr, \
-                                                    G5T<T>& dh, G5T<T>& gu, T& grr) {                \
-            (void)q; (void)dp; (void)dm;                                                             \
-            BODY                                                                                     \
-        }                                                                                            \
-    };
-
-FOORT_DEFINE_MIXED_METRIC(kKerr, FOORT_MIXED_BODY_KERR, true)
-FOORT_DEFINE_MIXED_METRIC(kJohannsen, FOORT_MIXED_BODY_JOHANNSEN, false)
-FOORT_DEFINE_MIXED_METRIC(kFlat, FOORT_MIXED_BODY_FLAT, true)
-
-// a^mu from d_1 g, d_2 g (derivatives in the integration coordinates x1, x2), g^uu, u.
-template <typename T>
-__device__ __forceinline__ void accel_lagrange(const G5T<T>& d1, const G5T<T>& d2, const G5T<T>& gu, const T u[4],
-                                               T a[4]) {
-    const T w1t = d1.tt * u[0] + d1.tp * u[3], w1r = d1.rr * u[1], w1h = d1.hh * u[2], w1p = d1.tp * u[0] + d1.pp * u[3];
-    const T w2t = d2.tt * u[0] + d2.tp * u[3], w2r = d2.rr * u[1], w2h = d2.hh * u[2], w2p = d2.tp * u[0] + d2.pp * u[3];
-    const T q1 = u[0] * w1t + u[1] * w1r + u[2] * w1h + u[3] * w1p;
-    const T q2 = u[0] * w2t + u[1] * w2r + u[2] * w2h + u[3] * w2p;
-    const T Ft = T(2) * (u[1] * w1t + u[2] * w2t);
-    const T Fp = T(2) * (u[1] * w1p + u[2] * w2p);
-    const T Fr = T(2) * (u[1] * w1r + u[2] * w2r) - q1;
-    const T Fh = T(2) * (u[1] * w1h + u[2] * w2h) - q2;
-    a[0] = T(-0.5) * (gu.tt * Ft + gu.tp * Fp);
-    a[3] = T(-0.5) * (gu.tp * Ft + gu.pp * Fp);
-    a[1] = T(-0.5) * gu.rr * Fr;
-    a[2] = T(-0.5) * gu.hh * Fh;
-}
-
 // Right-hand side at (x1, theta) with velocity u. `x1` is the compensated radial
 // coordinate (r, or ln r in log-r mode); r_+ / r_- (and their logarithms) come from the
 // image constants so that dp = r - r_+ and dm = r - r_- are accurate near the horizon.
@@ -134,14 +88,7 @@ __device__ __forceinline__ void rhs_analytic(const T* q, const MixedConst& mc, b
     G5T<T> dr, dh, gu;
     T grr;
     MixedMetric<MID>::template eval<T>(q, r, dp, dm, s, c, dr, dh, gu, grr);
-    if (rlog) {
-        // x1 = ln r: d_x1 = r d_r, g_11 = r^2 g_rr, g^11 = g^rr / r^2
-        const T r2 = r * r;
-        dr.tt *= r; dr.tp *= r; dr.hh *= r; dr.pp *= r;
-        dr.rr = r * (T(2) * r * grr + r2 * dr.rr);
-        dh.rr *= r2;
-        gu.rr /= r2;
-    }
+    if (rlog) to_log_r(r, grr, dr, dh, gu);
     accel_lagrange(dr, dh, gu, u, a);
 }
 
@@ -159,16 +106,21 @@ __device__ __noinline__ void rhs_fp64_path(const double* q, const MixedConst& mc
     for (int i = 0; i < 4; ++i) a[i] = static_cast<float>(ad[i]);
 }
 
-// Integrators::GetAdaptiveStep (Integrators.cpp:34-46) in FP32.
-__device__ __forceinline__ float adaptive_step_f32(const RunConst& R, float th, const float v[4]) {
-    const float eps = static_cast<float>(R.eps);
-    const float pi = static_cast<float>(kRefPi);
-    const float d1 = eps / (fabsf(v[1]) + 1e-20f);
+// Integrators::GetAdaptiveStep (Integrators.cpp:34-46) in FP32. Written as
+//     h = eps / ((|u1| + d) + (|u2| + d) / m + |u3 + d|),  m = min(theta, pi - theta),
+// which is the reference's expression with eps factored out, evaluated with correctly
+// rounded operations and eps carried as a float-float pair: the step size then has no
+// systematic bias against the FP64 kernel's (a bias would shift where along the ray
+// the last step lands).
+__device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const MixedConst& mc, float th, const float v[4]) {
+    const float pi = mc.pi[0];
     const float m = (pi - th < th) ? pi - th : th;
-    const float d2 = eps * m / (fabsf(v[2]) + 1e-20f);
-    const float d3 = eps / fabsf(v[3] + 1e-20f);
-    const float h = 1.f / (1.f / fabsf(d1) + 1.f / fabsf(d2) + 1.f / fabsf(d3));
-    const float hmin = static_cast<float>(R.hmin);
+    const float s1 = __fadd_rn(fabsf(v[1]), 1e-20f);
+    const float s2 = __fdiv_rn(__fadd_rn(fabsf(v[2]), 1e-20f), fabsf(m));
+    const float s3 = fabsf(__fadd_rn(v[3], 1e-20f));
+    const float inv = __frcp_rn(__fadd_rn(__fadd_rn(s1, s2), s3));
+    const float h = __fmaf_rn(mc.eps[0], inv, __fmul_rn(mc.eps[1], inv));
+    const float hmin = mc.hmin;
     return (h < hmin) ? hmin : h;
 }
 
@@ -316,7 +268,7 @@ struct MixedEngine {
 #pragma unroll
         for (int i = 0; i < 4; ++i) uf[i] = ff_f(L.v[i]);
         const float th0 = ff_f(L.x[2]);
-        const float h = adaptive_step_f32(R, th0, uf);
+        const float h = adaptive_step_f32(R, I.mx, th0, uf);
         float du[4];
         float dxc[4];  // O(h^2) part of the position increment
         if (INTEG == FOORT_INTEGRATOR_RK4) {
@@ -332,7 +284,10 @@ struct MixedEngine {
 #pragma unroll
             for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
             rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), th0 + h * (uf[2] + hh * k2[2]), us, k4);
-            const float h6 = h * (1.f / 6.f), hh6 = h * h6;
+            // h / 6 is divided, not multiplied by a rounded 1/6: that constant is 3e-8 too
+            // large, which would scale every velocity increment by the same factor and,
+            // amplified by strongly bent orbits, bias the escape direction by ~1e-7.
+            const float h6 = __fdiv_rn(h, 6.f), hh6 = __fmul_rn(h, h6);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 du[i] = h6 * (k1[i] + 2.f * k2[i] + 2.f * k3[i] + k4[i]);

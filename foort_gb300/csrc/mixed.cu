@@ -49,6 +49,8 @@ void fill_mixed_constants(int metric_id, ImageConst& ic, const RunConst& rc) {
     ff_split(kRefPi, mx.pi[0], mx.pi[1]);
     ff_split(-(kRefPi / 2.0), mx.mpio2[0], mx.mpio2[1]);
     ff_split(kRefPi / 2.0 * rc.eq_thr, mx.eqthr[0], mx.eqthr[1]);
+    ff_split(rc.eps, mx.eps[0], mx.eps[1]);
+    mx.hmin = static_cast<float>(rc.hmin);
 }
 
 }  // namespace foort

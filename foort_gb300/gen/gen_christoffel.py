@@ -94,22 +94,58 @@ def condition(e, dl):
     return sp.collect(num, r) / den
 
 
-def emit(name, gdd, guu, dl):
+u = sp.Symbol("u", positive=True)
+
+
+def condition_inv(e, dl):
+    """Like condition(), in the inverse radius u = 1/r: e = r^k P(u) / Q(u) with P and Q
+    polynomials whose terms are O(1) for every r >= r_+, so that FP32 neither overflows
+    (Johannsen's expanded numerators reach r^15) nor cancels large terms. A factor
+    Delta / r^2 = 1 - 2u + a^2 u^2 of Q is written dp * dm * u^2."""
+    e = sp.together(to_sc(e).subs(r, 1 / u))
+    num, den = sp.fraction(e)
+    num = sp.expand(sp.expand(num).subs(c**2, 1 - s**2))
+    den = sp.expand(den)
+    # pull the powers of u out of numerator and denominator
+    pn = sp.Poly(num, u)
+    pd = sp.Poly(den, u)
+    kn = min(m[0] for m in pn.monoms())
+    kd = min(m[0] for m in pd.monoms())
+    num = sp.expand(num / u**kn)
+    den = sp.expand(den / u**kd)
+    k = kn - kd  # e = u^k * num / den
+    dfac = 1
+    if dl is not None:
+        dlu = sp.expand(to_sc(dl).subs(r, 1 / u) * u**2)  # Delta / r^2 as a polynomial in u
+        pdl = sp.Poly(dlu, u)
+        while True:
+            q, rem = sp.div(sp.Poly(den, u), pdl)
+            if not rem.is_zero:
+                break
+            den = q.as_expr()
+            dfac = dfac * (dp * dm * u**2)
+    num = sp.horner(sp.collect(num, u), u) if num.has(u) else num
+    den = sp.horner(sp.collect(sp.expand(den), u), u) if sp.expand(den).has(u) else den
+    return u**k * num / (den * dfac)
+
+
+def emit(name, gdd, guu, dl, inv=False):
+    cond = condition_inv if inv else condition
     exprs = []
     names = []
     for k in COMP:
-        exprs.append(condition(sp.diff(gdd[k], r), dl))
+        exprs.append(cond(sp.diff(gdd[k], r), dl))
         names.append(f"dr.{k}")
     for k in COMP:
-        exprs.append(condition(sp.diff(gdd[k], th), dl))
+        exprs.append(cond(sp.diff(gdd[k], th), dl))
         names.append(f"dh.{k}")
     for k in COMP:
-        exprs.append(condition(guu[k], dl))
+        exprs.append(cond(guu[k], dl))
         names.append(f"gu.{k}")
-    exprs.append(condition(gdd["rr"], dl))
+    exprs.append(cond(gdd["rr"], dl))
     names.append("grr")
     repl, red = sp.cse(exprs, symbols=sp.numbered_symbols("t"), optimizations="basic")
-    lines = []
+    lines = ["const T u = T(1) / r;"] if inv else []
     for sym, e in repl:
         lines.append(f"const T {sym} = {ccode(e)};")
     for n, e in zip(names, red):
@@ -182,9 +218,11 @@ def main():
     print("// Generated by foort_gb300/gen/gen_christoffel.py -- do not edit.")
     print("// Inputs: q[] metric constants, r, dp = r - r_+, dm = r - r_-, s = sin(theta),")
     print("// c = cos(theta). Outputs: dr = d_r g_dd, dh = d_theta g_dd, gu = g^uu, grr = g_rr.")
-    for name, fn in (("Kerr", kerr), ("Johannsen", johannsen), ("Flat", flat)):
+    # Kerr's expanded numerators stay below r^8 and are emitted in r; Johannsen's are
+    # emitted in u = 1/r.
+    for name, fn, inv in (("Kerr", kerr, False), ("Johannsen", johannsen, True), ("Flat", flat, False)):
         gdd, guu, dl = fn()
-        body = emit(name, gdd, guu, dl)
+        body = emit(name, gdd, guu, dl, inv)
         print(f"#define FOORT_MIXED_BODY_{name.upper()} \\")
         print(" \\\n".join("    " + l for l in body.split("\n")))
         print()

@@ -237,6 +237,15 @@ double foort_horizon_radius(int32_t metric_id, const double* metric_params);
  * (Config.cpp:123-323, 985-1071). */
 int foort_gpu_has_kernel(int32_t metric_id, int32_t integrator_id, int32_t precision);
 
+/* Christoffel symbols gamma[16*mu + 4*nu + rho] at the point x (integration
+ * coordinates: x[1] = ln r when rlog) from the analytic metric derivatives the
+ * mixed-precision kernel uses, evaluated in FP64 on the host. Replaces
+ * Metric::getChristoffel_udd (Metric.cpp:14-55), which differentiates numerically.
+ * FOORT_E_UNSUPPORTED for metrics without an analytic plugin (Rasheed-Larsen,
+ * Manko-Novikov). */
+int foort_metric_christoffel(int32_t metric_id, const double* metric_params, int32_t rlog, const double* x,
+                             double* gamma);
+
 /* sizeof() of the ABI structs, for binding checks: 0 foort_pixel, 1 foort_result,
  * 2 foort_run_desc, 3 foort_image_desc, 4 foort_stats; 0 otherwise. Engine extension. */
 uint64_t foort_abi_size(int32_t which);
@@ -244,6 +253,45 @@ uint64_t foort_abi_size(int32_t which);
 /* Measured FP32 and FP64 FMA throughput of the current GPU in TFLOP/s (an FMA counts as
  * two operations): the denominators of the engine's ALU roofline. Engine extension. */
 int foort_measure_peaks(double* fp32_tflops, double* fp64_tflops);
+
+/* ---- meshes: which pixels each integration round gets --------------------------------
+ * Host-side counterparts of the reference's Mesh plugins (Mesh.h:24-61). A FOORT run is
+ *     while (!is_finished) { get_pixels; integrate; set_results; end_current_loop; }
+ * (Main.cpp:313-419). The adaptive mesh hands out exactly the reference's pixels, in the
+ * reference's order. */
+typedef struct foort_mesh foort_mesh;
+
+/* SimpleSquareMesh(totalPixels, valdiag), Mesh.h:73-82. diag_flags / value_diag are the
+ * run's (they select the value each geodesic reports to the mesh). */
+int foort_mesh_create_simple(uint64_t total_pixels, uint32_t diag_flags, uint32_t value_diag, foort_mesh** out);
+
+/* SquareSubdivisionMeshV2(maxPixels, initialPixels, maxSubdivide, iterationPixels,
+ * initialSubToFinal, valdiag), Mesh.h:301-315. */
+int foort_mesh_create_v2(uint64_t max_pixels, uint64_t initial_pixels, int32_t max_subdivide,
+                         uint64_t iteration_pixels, int32_t initial_sub_to_final, uint32_t diag_flags,
+                         uint32_t value_diag, foort_mesh** out);
+
+/* Mesh::IsFinished (1 / 0), Mesh::getCurNrGeodesics, the grid size R of the unit
+ * screen point (row, col) / (R - 1), and the number of completed rounds. */
+int foort_mesh_is_finished(const foort_mesh* mesh);
+uint64_t foort_mesh_cur_nr_geodesics(const foort_mesh* mesh);
+uint64_t foort_mesh_grid(const foort_mesh* mesh);
+uint64_t foort_mesh_rounds(const foort_mesh* mesh);
+
+/* Mesh::getNewInitConds for every index of the current round, as pixels of `image`. */
+int foort_mesh_get_pixels(const foort_mesh* mesh, uint32_t image, foort_pixel* out);
+
+/* Mesh::GeodesicFinished(index, values) (Mesh.h:44-46). */
+int foort_mesh_geodesic_finished(foort_mesh* mesh, uint64_t index, const double* values, uint32_t n_values);
+
+/* GeodesicFinished for the whole round from the integration results: each geodesic's
+ * value is Geodesic::getDiagnosticFinalValue() (Geodesic.cpp:141-149). */
+int foort_mesh_set_results(foort_mesh* mesh, const foort_result* results, uint64_t n);
+
+/* Mesh::EndCurrentLoop: weights, ordering and subdivision of the next round. */
+int foort_mesh_end_current_loop(foort_mesh* mesh);
+
+void foort_mesh_destroy(foort_mesh* mesh);
 
 #ifdef __cplusplus
 }

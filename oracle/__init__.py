@@ -127,4 +127,4 @@ def synth_value(kind, row, col, grid):
         v = (row * 31 + col * 17) // w
         return float(v % 6 - 2)
     h = (row * 7919 + col * 104729) % 1009
-    return 1.5 + float(h) / 1009.0 * float((row + col) % 3)
+    return 1.5 + float(h) * 0.0009765625 * float((row + col) % 3)

@@ -297,9 +297,10 @@ static double synth_value(int kind, uint64_t row, uint64_t col, uint64_t grid) {
         long long w = R / 8 + 1;
         return static_cast<double>(((static_cast<long long>(row) * 31 + static_cast<long long>(col) * 17) / w) % 6 - 2);
     }
-    // radius-like continuous values
+    // radius-like continuous values; every operation is exact (a power-of-two scale),
+    // so the value does not depend on floating-point flags
     long long h = (static_cast<long long>(row) * 7919 + static_cast<long long>(col) * 104729) % 1009;
-    return 1.5 + static_cast<double>(h) / 1009.0 * static_cast<double>((row + col) % 3);
+    return 1.5 + static_cast<double>(h) * 0.0009765625 * static_cast<double>((row + col) % 3);
 }
 
 // Drive a reference Mesh with synthetic values and record every round's queue:

@@ -1,0 +1,91 @@
+// FP32 accuracy of the analytic metric plugins (built and run by
+// tests/test_analytic_metrics.py).
+//
+// For each metric, random points r in [r_+ + 0.01, 1000] (log-uniform) and theta, and
+// random null velocities, the geodesic acceleration is evaluated with the plugin in
+// double and in float (the float inputs prepared as the mixed kernel prepares them:
+// r - r_+ and r - r_- from the exact radius, then rounded). Output, one line per case:
+//   name p50 p90 p99 max
+// of |a_float - a_double| / |a_double|_inf.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <random>
+#include <vector>
+
+#include "../foort_gb300/csrc/analytic_metric.cuh"
+
+using namespace foort;
+
+template <int MID>
+void run(const char* name, const double* params, bool rlog) {
+    MetricConst M = make_metric_const(MID, params);
+    double rp = 0.0, rm = 0.0;
+    if (MID == kKerr || MID == kJohannsen) {
+        rp = 1.0 + std::sqrt(1.0 - params[0] * params[0]);
+        rm = 1.0 - std::sqrt(1.0 - params[0] * params[0]);
+    }
+    float qf[6];
+    for (int i = 0; i < 6; ++i) qf[i] = static_cast<float>(M.q[i]);
+    std::mt19937_64 rng(7);
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    std::vector<double> errs;
+    const double rlo = (rp > 0 ? rp : 1.0) + 0.01;
+    for (int k = 0; k < 20000; ++k) {
+        const double r = rlo * std::pow(1000.0 / rlo, U(rng));
+        const double th = 0.05 + (M_PI - 0.1) * U(rng);
+        const double s = std::sin(th), c = std::cos(th);
+        G5T<double> dr, dh, gu;
+        double grr;
+        MixedMetric<MID>::template eval<double>(M.q, r, r - rp, r - rm, s, c, dr, dh, gu, grr);
+        G5 g = metric_dd_host(MID, M, r, s, c, false);
+        // random spatial direction, u^t from the null condition with E = -u_t ~ 1
+        double ur = 2 * U(rng) - 1, uh = (2 * U(rng) - 1) / r, up = (2 * U(rng) - 1) / (r * (s + 1e-3));
+        double A = g.tt, B = 2 * g.tp * up, Cc = g.rr * ur * ur + g.hh * uh * uh + g.pp * up * up;
+        double disc = B * B - 4 * A * Cc;
+        if (disc < 0) continue;
+        double ut = (-B - std::sqrt(disc)) / (2 * A);
+        double u[4] = {ut, ur, uh, up};
+        if (rlog) {
+            to_log_r(r, grr, dr, dh, gu);
+            u[1] = ur / r;  // d ln r / d lambda
+        }
+        double ad[4];
+        accel_lagrange(dr, dh, gu, u, ad);
+        // float path
+        float rf = static_cast<float>(r), dpf = static_cast<float>(r - rp), dmf = static_cast<float>(r - rm);
+        float sf = std::sin(static_cast<float>(th)), cf = std::cos(static_cast<float>(th));
+        G5T<float> fr, fh, fu;
+        float frr;
+        MixedMetric<MID>::template eval<float>(qf, rf, dpf, dmf, sf, cf, fr, fh, fu, frr);
+        if (rlog) to_log_r(rf, frr, fr, fh, fu);
+        float uf[4] = {static_cast<float>(u[0]), static_cast<float>(u[1]), static_cast<float>(u[2]), static_cast<float>(u[3])};
+        float af[4];
+        accel_lagrange(fr, fh, fu, uf, af);
+        double scale = 0, diff = 0;
+        for (int i = 0; i < 4; ++i) {
+            scale = std::max(scale, std::fabs(ad[i]));
+            diff = std::max(diff, std::fabs(static_cast<double>(af[i]) - ad[i]));
+        }
+        if (!(scale > 0)) continue;
+        errs.push_back(std::isfinite(diff) ? diff / scale : 1e30);
+    }
+    std::sort(errs.begin(), errs.end());
+    auto q = [&](double f) { return errs[static_cast<size_t>(f * (errs.size() - 1))]; };
+    std::printf("%s %.3e %.3e %.3e %.3e\n", name, q(0.5), q(0.9), q(0.99), errs.back());
+}
+
+int main() {
+    const double kerr99[6] = {0.99}, kerr5[6] = {0.5}, kerr998[6] = {0.998};
+    const double joh_c4[6] = {0.9, -0.5, 0, 0, 0}, joh_test[6] = {0.7, 2.0, 0, 0, 0}, joh_all[6] = {0.8, 1.0, 0.5, 0.2, 0.1};
+    const double none[6] = {0};
+    run<kKerr>("kerr_a0.99", kerr99, false);
+    run<kKerr>("kerr_a0.5", kerr5, false);
+    run<kKerr>("kerr_a0.998", kerr998, false);
+    run<kKerr>("kerr_a0.5_logr", kerr5, true);
+    run<kJohannsen>("johannsen_c4", joh_c4, false);
+    run<kJohannsen>("johannsen_test_logr", joh_test, true);
+    run<kJohannsen>("johannsen_all_params", joh_all, false);
+    run<kFlat>("flat", none, false);
+    return 0;
+}
