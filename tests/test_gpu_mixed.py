@@ -1,0 +1,127 @@
+"""GPU parity of the mixed-precision kernel (-m gpu), through the C ABI.
+
+Against the reference (shipped golden files and reference fixtures): the discrete
+outputs, with the rules of foort_gb300/accuracy.py (>= 99.9 % agreement, every
+disagreement on a decision boundary). Against the FP64 kernel on the same pixels: the
+relative endpoint error e (accuracy.endpoint_rel_err) on pixels with the same discrete
+outputs and step count, bounded per workload by the tolerances below.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import parity
+from conftest import GOLDEN
+from foort_gb300 import abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+# Endpoint error of the mixed kernel against the FP64 kernel (median, p90). The FP32
+# right-hand side has ~1e-7 relative error per evaluation; compensated state and
+# unbiased step arithmetic keep the accumulated endpoint error near that level.
+MIXED_MEDIAN_TOL = 1e-6
+MIXED_P90_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def eng():
+    import foort_gb300
+    from foort_gb300 import build as engine_build
+    engine_build.build()
+    foort_gb300.check_layout()
+    if not foort_gb300.mixed_available():
+        pytest.fail("the mixed-precision kernels are missing from this build")
+    return foort_gb300
+
+
+def run(eng, desc, px, precision, options=0):
+    desc.precision = precision
+    desc.mixed_options = options
+    with eng.Engine(desc) as e:
+        r = e.integrate(px)
+        return r, e.stats()
+
+
+@pytest.mark.parametrize("name", ["test", "debug"])
+@pytest.mark.parametrize("options", [0, abi.MIXED_FF_DECISIONS])
+def test_mixed_reproduces_shipped_golden(eng, oracle_mod, name, options):
+    """FOORT/Output/{Test,debug}_*.dat: Johannsen, log-r, Verlet / RK4, 62,500 pixels."""
+    g = np.load(os.path.join(GOLDEN, f"johannsen_{name}.npz"))
+    wl = workloads.johannsen_golden(name == "test")
+    px = abi.square_pixels(250)
+    res, st = run(eng, wl.desc, px, abi.PREC_MIXED, options)
+    mism = (res["quadrant"] != g["quadrant"]) | (res["equat_passes"] != g["passes"])
+    agree = 1.0 - mism.mean()
+    print(f"{name} options={options}: agreement {agree:.6f} ({mism.sum()} differ), {st['kernel_ms']:.1f} ms")
+    assert agree >= parity.MIN_DISCRETE_AGREEMENT
+    wl.desc.precision = abi.PREC_FP64
+    ref = oracle_mod.integrate(wl.desc, px[mism], fast=True)
+    real = np.zeros(len(px), dtype=bool)
+    real[np.nonzero(mism)[0]] = parity.discrete_mismatch(res[mism], ref)
+    unexplained = parity.explain_mismatches(oracle_mod, wl.desc, px, res, real)
+    assert len(unexplained) == 0, unexplained
+
+
+CASES = {"c1": lambda: workloads.c1(), "c2": lambda: workloads.c2(), "c3": lambda: workloads.c3(n_images=64),
+         "c4": lambda: workloads.c4(), "debug_sample": lambda: workloads.johannsen_golden(False)}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_mixed_vs_reference_and_fp64(eng, oracle_mod, case):
+    f = np.load(os.path.join(GOLDEN, f"ref_{case}.npz"))
+    wl = CASES[case]()
+    if case in ("c2", "c4"):
+        wl.desc.value_diag = abi.DIAG_CLOSEST_RADIUS
+    px, ref = f["px"], f["fast"]
+    res, _ = run(eng, wl.desc, px, abi.PREC_MIXED)
+    r64, _ = run(eng, wl.desc, px, abi.PREC_FP64)
+    wl.desc.precision = abi.PREC_FP64
+    mism = parity.discrete_mismatch(res, ref)
+    unexplained = parity.explain_mismatches(oracle_mod, wl.desc, px, res, mism)
+    print(f"{case}: agreement with the reference {1 - mism.mean():.4f}")
+    assert len(unexplained) == 0, unexplained
+    m64 = parity.discrete_mismatch(res, r64)
+    same = (~m64) & (res["steps"] == r64["steps"])
+    s = parity.summarize(parity.endpoint_rel_err(res[same], r64[same], rlog=bool(wl.desc.rlog)))
+    print(f"{case}: vs FP64 kernel: agreement {1 - m64.mean():.4f}, same steps {same.mean():.4f}, endpoint {s}")
+    assert s["median"] < MIXED_MEDIAN_TOL and s["p90"] < MIXED_P90_TOL, s
+
+
+def test_mixed_large_sample_vs_fp64(eng):
+    """8,000 pixels of the C2 grid: the statistic the benchmark reports."""
+    wl = workloads.c2()
+    rng = np.random.default_rng(11)
+    idx = np.sort(rng.choice(509 * 509, 8000, replace=False))
+    px = np.zeros(len(idx), dtype=abi.PIXEL_DTYPE)
+    px["row"], px["col"], px["grid"] = idx // 509, idx % 509, 509
+    res, sm = run(eng, wl.desc, px, abi.PREC_MIXED)
+    r64, s64 = run(eng, wl.desc, px, abi.PREC_FP64)
+    m64 = parity.discrete_mismatch(res, r64)
+    same = (~m64) & (res["steps"] == r64["steps"])
+    err = parity.endpoint_rel_err(res[same], r64[same])
+    s = parity.summarize(err)
+    print(f"C2 sample: agreement {1 - m64.mean():.5f}; endpoint {s}; <=1e-6: {np.mean(err <= 1e-6):.4f}; "
+          f"speed-up {s64['kernel_ms'] / sm['kernel_ms']:.1f}x")
+    assert 1 - m64.mean() >= parity.MIN_DISCRETE_AGREEMENT
+    assert s["median"] < MIXED_MEDIAN_TOL and s["p90"] < MIXED_P90_TOL
+
+
+def test_mixed_budget_and_cancel_paths(eng):
+    wl = workloads.c1(precision=abi.PREC_MIXED)
+    px = abi.square_pixels(60)
+    with eng.Engine(wl.desc) as e:
+        e.set_budget(100000)
+        res = e.integrate(px, allow=(abi.FOORT_E_BUDGET,))
+        assert e.stats()["status"] != 0
+    assert np.any(res["err"] & (abi.ERR_BUDGET | abi.ERR_UNFINISHED))
+
+
+def test_unsupported_metric_for_mixed(eng):
+    d = workloads.base_desc(abi.PREC_MIXED)
+    d.metric_id = abi.METRIC_MANKO_NOVIKOV
+    keep = abi.attach_images(d, [abi.make_image((0.9, 1.0))])
+    with pytest.raises(eng.FoortError) as e:
+        eng.Engine(d)
+    assert e.value.code == abi.FOORT_E_UNSUPPORTED
+    del keep
