@@ -241,6 +241,8 @@ def run_profile_case(args):
     from foort_gb300 import abi
     out = {}
     for prec, name in ((abi.PREC_MIXED, "mixed"), (abi.PREC_FP64, "fp64")):
+        if args.profile_precision not in ("both", name):
+            continue
         wl = workload(args.workload, prec, args.iteration_pixels)
         kind, spec = wl.mesh[0]
         side = spec if kind == "simple" else int((math.sqrt(spec["initial_pixels"]) - 1) * 2 ** (spec["max_subdivide"] - 1) + 1)
@@ -297,6 +299,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--profile-precision", default="both", choices=["both", "mixed", "fp64"])
     ap.add_argument("--profile", type=int, default=0, metavar="N",
                     help="profiling case: one launch of the mixed and one of the FP64 kernel on N pixels of "
                          "the workload's grid (after one warm-up launch each), then exit")

@@ -29,7 +29,7 @@ INTEGRATOR_VERLET = 1
 PREC_FP64 = 0
 PREC_MIXED = 1
 
-MIXED_FF_DECISIONS = 0x1
+MIXED_FP64_DECISIONS = 0x1
 MIXED_FP64_NEAR_HORIZON = 0x2
 
 # TermBitflag (Terminations.h:29-33)

@@ -19,6 +19,17 @@ struct G5T {
     T tt, tp, rr, hh, pp;
 };
 
+// Correctly rounded reciprocal: the generated bodies multiply by reciprocals of their
+// denominators' factors instead of dividing.
+FOORT_HD float rcp(float x) {
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(x);
+#else
+    return 1.0f / x;
+#endif
+}
+FOORT_HD double rcp(double x) { return 1.0 / x; }
+
 template <int MID>
 struct MixedMetric {
     static constexpr bool kAvailable = false;

@@ -196,7 +196,7 @@ RunConst make_run_const(const foort_run_desc& d) {
 
 const void* select_kernel(const RunConst& R) {
     if (R.precision == FOORT_PREC_MIXED)
-        return mixed_kernel_variant(R.metric_id, R.integrator, !(R.mixed_options & FOORT_MIXED_FF_DECISIONS));
+        return mixed_kernel_variant(R.metric_id, R.integrator, (R.mixed_options & FOORT_MIXED_FP64_DECISIONS) != 0);
     return fp64_kernel(R.metric_id, R.integrator);
 }
 

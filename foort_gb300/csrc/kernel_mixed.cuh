@@ -357,8 +357,10 @@ struct MixedEngine {
         ++L.steps;
         L.term = terms(L, I, R);
         diags(L, I, R, false);
-        if (!(isfinite(L.x[1].hi) && isfinite(L.x[2].hi) && isfinite(L.v[1].hi) && isfinite(L.v[2].hi) &&
-              isfinite(L.x[0].hi) && isfinite(L.x[3].hi) && isfinite(L.v[0].hi) && isfinite(L.v[3].hi))) {
+        // A NaN or Inf anywhere in the state reaches r or u^r within one step through the
+        // right-hand side, so those two words stand for the whole state here; the full
+        // state is checked again when the geodesic's record is written.
+        if (!(isfinite(L.x[1].hi) && isfinite(L.v[1].hi))) {
             L.err |= FOORT_ERR_NONFINITE;
             if (L.term == FOORT_TERMCODE_CONTINUE && !(R.term_flags & FOORT_TERM_TIMEOUT)) return false;
         }
@@ -369,6 +371,7 @@ struct MixedEngine {
                                                  uint32_t err) {
         double x[4], v[4];
         load_double(L, x, v);
+        if (!(finite4(x) && finite4(v))) err |= FOORT_ERR_NONFINITE;
         DiagState D;
         D.quad = L.quad;
         D.passes = L.passes;

@@ -21,6 +21,21 @@ import sympy as sp
 
 r, th, s, c, dp, dm = sp.symbols("r theta s c dp dm", real=True)
 COMP = ["tt", "tp", "rr", "hh", "pp"]
+# Every denominator is applied as a product of reciprocals of its factors, rcp(x) =
+# correctly rounded 1/x (one per distinct factor after common-subexpression
+# elimination) instead of an IEEE division per expression: fewer long dependency
+# chains, and every rounding stays unbiased.
+rcp = sp.Function("rcp")
+
+
+def with_reciprocals(num, den):
+    out = num
+    for base, k in sp.factor(den).as_powers_dict().items():
+        if base.is_number:
+            out = out / base**k
+        else:
+            out = out * rcp(base)**k
+    return out
 
 
 def kerr():
@@ -91,7 +106,7 @@ def condition(e, dl):
                 dd = qq.as_expr()
                 k += 1
             den = dd * (dp * dm)**k
-    return sp.collect(num, r) / den
+    return with_reciprocals(sp.collect(num, r), den)
 
 
 u = sp.Symbol("u", positive=True)
@@ -126,7 +141,7 @@ def condition_inv(e, dl):
             dfac = dfac * (dp * dm * u**2)
     num = sp.horner(sp.collect(num, u), u) if num.has(u) else num
     den = sp.horner(sp.collect(sp.expand(den), u), u) if sp.expand(den).has(u) else den
-    return u**k * num / (den * dfac)
+    return with_reciprocals(u**k * num, den * dfac)
 
 
 def emit(name, gdd, guu, dl, inv=False):
@@ -201,6 +216,8 @@ def ccode(e):
             if den:
                 s_ = f"({s_})/({'*'.join(den)})"
             return f"({s_})"
+        if isinstance(x, sp.Function) and x.func == rcp:
+            return f"rcp({p(x.args[0])})"
         if isinstance(x, sp.Pow):
             if x.exp.is_Integer:
                 n = int(x.exp)

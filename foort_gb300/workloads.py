@@ -120,7 +120,7 @@ def c1(precision=abi.PREC_FP64, side=100):
 
 # IterationPixels of C2: chosen so that the run is the seed round plus exactly four
 # refinement rounds.
-C2_ITERATION_PIXELS = 3000
+C2_ITERATION_PIXELS = 800
 
 
 def c2(precision=abi.PREC_FP64, iteration_pixels=None):

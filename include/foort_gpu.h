@@ -55,9 +55,10 @@ extern "C" {
 #define FOORT_PREC_MIXED 1 /* FP32 bulk with compensated state, FP64 where needed       */
 
 /* Options of the mixed-precision kernel (engine extension). By default its decisions
- * (terminations, equator crossings, closest radius) are taken in FP64 on the exact
- * double value of its compensated state. */
-#define FOORT_MIXED_FF_DECISIONS 0x1u      /* take them in float-float arithmetic instead */
+ * (terminations, equator crossings, closest radius) are taken by float-float
+ * comparisons of its compensated (48-bit) state, which agree with FP64 comparisons
+ * except within 2^-48 (relative) of a threshold. */
+#define FOORT_MIXED_FP64_DECISIONS 0x1u    /* take them in FP64 on the exact double value  */
 #define FOORT_MIXED_FP64_NEAR_HORIZON 0x2u /* FP64 right-hand side near the horizon       */
 
 /* TermBitflag, Terminations.h:29-33 */

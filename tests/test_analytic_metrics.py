@@ -1,0 +1,57 @@
+"""Analytic metric plugins of the mixed-precision kernel (CPU).
+
+* In FP64 they must equal the reference's finite-difference Christoffel symbols
+  (Metric.cpp:14-55, restated by the oracle) to the finite differences' own accuracy.
+* In FP32 (tests/analytic_check.cpp, the same plugin code the kernel runs) the
+  geodesic acceleration must keep FP32 accuracy from r_+ + 0.01 to 1000: no overflow
+  (Johannsen's expanded numerators would reach r^15) and no near-horizon cancellation.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+CASES = [(0, (0.99,), 0), (0, (0.7,), 1), (3, (0.9, -0.6, 0, 0, 0), 0), (3, (0.7, 2.0, 0, 0, 0), 1),
+         (3, (0.8, 1.0, 0.5, 0.2, 0.1), 0), (1, (), 0)]
+
+
+@pytest.mark.parametrize("metric,params,rlog", CASES)
+def test_analytic_christoffel_equals_finite_differences(engine_lib, oracle_mod, metric, params, rlog):
+    ol = oracle_mod.oracle_lib()
+    p = np.zeros(6)
+    p[:len(params)] = params
+    rng = np.random.default_rng(1)
+    worst = 0.0
+    for _ in range(300):
+        r = 10 ** rng.uniform(0.3, 3)
+        th = rng.uniform(0.1, 3.0)
+        x = np.array([0.0, np.log(r) if rlog else r, th, 0.3])
+        ga, gb = np.zeros(64), np.zeros(64)
+        assert engine_lib.foort_metric_christoffel(metric, p.ctypes.data, rlog, x.ctypes.data, ga.ctypes.data) == 0
+        ol.oracle_christoffel(metric, p.ctypes.data, rlog, 1e-5, x.ctypes.data, gb.ctypes.data)
+        worst = max(worst, np.abs(ga - gb).max() / np.abs(gb).max())
+    assert worst < 1e-7, worst
+
+
+def test_no_analytic_plugin_for_rasheed_larsen_and_manko_novikov(engine_lib):
+    p = np.array([0.94, 13.0, 0, 0, 0, 0.0])
+    x = np.array([0.0, 10.0, 1.0, 0.0])
+    g = np.zeros(64)
+    assert engine_lib.foort_metric_christoffel(4, p.ctypes.data, 0, x.ctypes.data, g.ctypes.data) == -6
+
+
+def test_fp32_acceleration_accuracy(tmp_path):
+    exe = tmp_path / "analytic_check"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-o", str(exe),
+                    os.path.join(ROOT, "tests", "analytic_check.cpp")], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    for line in out.strip().splitlines():
+        name, p50, p90, p99, mx = line.split()
+        p50, p99, mx = float(p50), float(p99), float(mx)
+        print(line)
+        # FP32 has 6e-8 unit roundoff; a few operations deep the acceleration keeps ~1e-7
+        assert p50 < 3e-7 and p99 < 3e-6 and mx < 1e-4, line

@@ -44,7 +44,7 @@ def run(eng, desc, px, precision, options=0):
 
 
 @pytest.mark.parametrize("name", ["test", "debug"])
-@pytest.mark.parametrize("options", [0, abi.MIXED_FF_DECISIONS])
+@pytest.mark.parametrize("options", [0, abi.MIXED_FP64_DECISIONS])
 def test_mixed_reproduces_shipped_golden(eng, oracle_mod, name, options):
     """FOORT/Output/{Test,debug}_*.dat: Johannsen, log-r, Verlet / RK4, 62,500 pixels."""
     g = np.load(os.path.join(GOLDEN, f"johannsen_{name}.npz"))
