@@ -38,6 +38,7 @@ def load():
     lib.foort_gpu_create.argtypes = [C.POINTER(abi.RunDesc), C.POINTER(vp)]
     lib.foort_gpu_integrate.argtypes = [vp, vp, u64, vp]
     lib.foort_gpu_integrate_async.argtypes = [vp, vp, u64, vp, vp]
+    lib.foort_gpu_integrate_noalloc.argtypes = [C.POINTER(abi.RunDesc), vp, u64, vp, vp, C.POINTER(abi.Stats)]
     lib.foort_gpu_sync.argtypes = [vp]
     lib.foort_gpu_set_budget.argtypes = [vp, u64]
     lib.foort_gpu_cancel.argtypes = [vp]

@@ -32,6 +32,9 @@ PREC_MIXED = 1
 MIXED_FP64_DECISIONS = 0x1
 MIXED_FP64_NEAR_HORIZON = 0x2
 
+# foort_gpu_integrate_noalloc: images its static device array has room for
+NOALLOC_MAX_IMAGES = 256
+
 # TermBitflag (Terminations.h:29-33)
 TERM_BOUNDARY_SPHERE = 0x1
 TERM_TIMEOUT = 0x2

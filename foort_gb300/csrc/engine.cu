@@ -479,3 +479,129 @@ const void* fp64_kernel(int metric_id, int integ) {
 }
 
 }  // namespace foort
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free entry point (foort_gpu_integrate_noalloc).
+//
+// The launch counters and the per-image constants that foort_gpu_create() puts in
+// cudaMalloc'd memory live here in one statically declared device array instead. On the
+// host, foort_noalloc_scratch names that array only as a symbol: its device address on
+// the current device comes from cudaGetSymbolAddress, looked up once per device.
+
+static_assert(sizeof(ImageConst) == 448, "FOORT_NOALLOC_SCRATCH_BYTES assumes 448-byte image constants");
+static_assert(kNumCtr * sizeof(unsigned long long) <= 256, "the counters take the first 256 bytes");
+
+static __device__ __align__(256) unsigned char foort_noalloc_scratch[FOORT_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+
+struct NoAllocDevice {
+    unsigned char* scratch = nullptr;  // device address of foort_noalloc_scratch
+    int num_sms = 0;
+};
+
+std::mutex g_noalloc_mu;
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+// Set-up of the current device, on its first call: the array's device address and the
+// SM count. Takes no stream operation.
+int noalloc_device(int dev, NoAllocDevice& out) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoAllocDevice& d = g_noalloc_dev[dev];
+    if (!d.scratch) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, foort_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(foort_noalloc_scratch)");
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaDeviceGetAttribute");
+        d.num_sms = sms;
+        d.scratch = static_cast<unsigned char*>(p);
+    }
+    out = d;
+    return FOORT_OK;
+}
+
+}  // namespace
+
+extern "C" int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foort_pixel* d_px, uint64_t n,
+                                           foort_result* d_out, void* cuda_stream, foort_stats* stats) {
+    foort_ctx* ctx = nullptr;  // errors go to foort_gpu_last_error(NULL)
+    std::string why;
+    int v = validate(desc, why);
+    if (v) return fail(nullptr, v, why);
+    if (desc->n_images > FOORT_NOALLOC_MAX_IMAGES)
+        return fail(nullptr, FOORT_E_BADARG,
+                    "n_images = " + std::to_string(desc->n_images) + " exceeds the " +
+                        std::to_string(FOORT_NOALLOC_MAX_IMAGES) +
+                        " images that the allocation-free entry point has room for");
+    if (n && (!d_px || !d_out)) return fail(nullptr, FOORT_E_BADARG, "NULL pixel or result buffer");
+    const RunConst R0 = make_run_const(*desc);
+    const void* fn = select_kernel(R0);
+    if (!fn) return fail(nullptr, FOORT_E_UNSUPPORTED, "no kernel for this metric / integrator / precision");
+
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return fail(nullptr, FOORT_E_BADARG, "device index beyond the " + std::to_string(kNoAllocMaxDevices) +
+                                                 " devices the allocation-free entry point tracks");
+    NoAllocDevice nd;
+    int rc = noalloc_device(dev, nd);
+    if (rc) return rc;
+    unsigned long long* d_ctr = reinterpret_cast<unsigned long long*>(nd.scratch);
+    ImageConst* d_images = reinterpret_cast<ImageConst*>(nd.scratch + 256);
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+
+    // Image constants, one at a time from the stack: a copy from pageable memory returns
+    // once the source has been staged, so the next image may reuse the buffer.
+    for (uint32_t i = 0; i < desc->n_images; ++i) {
+        ImageConst ic;
+        std::memset(&ic, 0, sizeof(ic));
+        ic.m = make_metric_const(desc->metric_id, desc->images[i].metric_params);
+        camera_frame(desc->metric_id, R0.rlog != 0, desc->images[i], ic);
+        ic.h_eps = desc->images[i].horizon_eps > 0.0 ? desc->images[i].horizon_eps : desc->horizon_eps;
+        if (R0.precision == FOORT_PREC_MIXED) fill_mixed_constants(desc->metric_id, ic, R0);
+        CK(cudaMemcpyAsync(d_images + i, &ic, sizeof(ic), cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemsetAsync(d_ctr, 0, kNumCtr * sizeof(unsigned long long), st));
+
+    const uint32_t bs = 128;
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, static_cast<int>(bs), 0));
+    if (per_sm <= 0) return fail(nullptr, FOORT_E_CUDA, "kernel does not fit on an SM with this block size");
+    const uint64_t full = static_cast<uint64_t>(per_sm) * static_cast<uint64_t>(nd.num_sms);
+    const uint64_t need = (n + bs - 1) / bs;
+    const uint32_t grid = static_cast<uint32_t>(std::max<uint64_t>(1, std::min(full, need)));
+    LaunchArgs A{};
+    A.px = d_px;
+    A.out = d_out;
+    A.n = n;
+    A.images = d_images;
+    A.n_images = desc->n_images;
+    A.ctr = d_ctr;
+    A.cancel = nullptr;
+    A.budget = 0;
+    if (!(R0.term_flags & FOORT_TERM_TIMEOUT)) A.budget = std::max<unsigned long long>(100000000ull, 1000000ull * n);
+    RunConst R = R0;
+    void* args[2] = {&A, &R};
+    if (n > 0) CK(cudaLaunchKernel(fn, dim3(grid), dim3(bs), args, 0, st));
+    if (!stats) return FOORT_OK;
+
+    unsigned long long h_ctr[kNumCtr] = {};
+    CK(cudaMemcpyAsync(h_ctr, d_ctr, sizeof(h_ctr), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::memset(stats, 0, sizeof(*stats));
+    stats->geodesics = h_ctr[kCtrDone];
+    stats->steps = h_ctr[kCtrSteps];
+    stats->rhs_evals = h_ctr[kCtrRhs];
+    stats->fp64_steps = h_ctr[kCtrFp64Steps];
+    stats->n_blocks = grid;
+    stats->block_size = bs;
+    rc = FOORT_OK;
+    if (h_ctr[kCtrStatus] & kStatusBudget)
+        rc = fail(nullptr, FOORT_E_BUDGET, "global step budget exhausted; unfinished geodesics are marked");
+    stats->status = static_cast<uint32_t>(rc);
+    return rc;
+}

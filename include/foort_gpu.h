@@ -205,6 +205,40 @@ int foort_gpu_integrate(foort_ctx* ctx, const foort_pixel* px, uint64_t n, foort
 int foort_gpu_integrate_async(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n,
                               foort_result* d_out, void* cuda_stream);
 
+/* Allocation-free integration. No counterpart in the reference, which has no device code.
+ *
+ * For callers that may not allocate device memory: a plugin inside an application whose
+ * pool allocator owns all of the GPU's memory and hands its plugins buffers rather than
+ * the right to call cudaMalloc, or a pipeline that cannot take the device-wide
+ * synchronisation that cudaMalloc / cudaFree may cause. foort_gpu_create() allocates its
+ * image constants and launch counters with cudaMalloc; this call keeps them instead in
+ * one fixed array of device memory that the library declares statically, of
+ * FOORT_NOALLOC_SCRATCH_BYTES (room for FOORT_NOALLOC_MAX_IMAGES images). Every GPU on
+ * which the library's device code is loaded holds that array until the process exits.
+ *
+ * The same kernels as foort_gpu_integrate_async() integrate n pixels from the DEVICE
+ * buffer d_px into the DEVICE buffer d_out (both the caller's), on `cuda_stream`
+ * (a cudaStream_t, 0 = legacy). The call allocates nothing on the device: no cudaMalloc,
+ * cudaFree or allocating library routine. It copies the image constants into the array
+ * and zeroes the counters on the stream before the launch.
+ *   - More than FOORT_NOALLOC_MAX_IMAGES images: FOORT_E_BADARG, and nothing is launched.
+ *   - The first call on a device, made with that device current, looks up the array's
+ *     device address (cudaGetSymbolAddress) and keeps it. Make that first call before
+ *     any stream capture.
+ *   - All calls share the one array, which keeps the last call's contents. Calls whose
+ *     work overlaps on the GPU (different streams, or other host threads) race on it
+ *     and give wrong results. Calls in sequence on one stream are safe.
+ *   - stats == NULL: the call returns once the work is enqueued. Per-geodesic outcomes
+ *     are in d_out[i].err.
+ *   - stats != NULL: the call waits for the stream. It fills stats (kernel_ms = 0: no
+ *     events are recorded) and returns the launch status, as foort_gpu_sync() does.
+ * There is no cancel flag; the step budget follows foort_gpu_integrate()'s default.
+ * Errors are reported through foort_gpu_last_error(NULL). */
+#define FOORT_NOALLOC_MAX_IMAGES 256u
+#define FOORT_NOALLOC_SCRATCH_BYTES (256u + 448u * FOORT_NOALLOC_MAX_IMAGES) /* 114,944 */
+int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foort_pixel* d_px, uint64_t n,
+                                foort_result* d_out, void* cuda_stream, foort_stats* stats);
+
 /* Wait for the last async launch of this context and return its status. */
 int foort_gpu_sync(foort_ctx* ctx);
 
