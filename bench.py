@@ -491,7 +491,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "mixed-f32 (float-float state, f64 decisions)", "data": "synthetic",
+        "vs_baseline": None, "dtype": "mixed-f32 (FP32 right-hand side; float-float state and decisions)", "data": "synthetic",
         "config": config_block(wl, args, rounds=len(rounds), geod=n_geod),
         "geodesics_per_step": world * n_geod, "steps_per_s": world * steps_total / (t_step * 1e-3),
         "gpu_launches": args.steps * len(rounds),

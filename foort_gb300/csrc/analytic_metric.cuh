@@ -30,6 +30,38 @@ FOORT_HD float rcp(float x) {
 }
 FOORT_HD double rcp(double x) { return 1.0 / x; }
 
+// sin and cos of a float-float angle theta = th_hi + th_lo, to FP32 relative accuracy
+// also where the result is tiny (sin near theta = 0 and pi, cos near pi/2). A float theta
+// cannot give that: its rounding error (up to 1.2e-7 near pi) exceeds the distance to
+// the pole of rays that pass it closely, and cos(float(pi/2)) = -4.4e-8 pulls rays out of
+// the equatorial plane. The angle is reduced against pi/2 split into three floats (the
+// true pi: the metric's poles are at the true 0 and pi), d = theta - k pi/2, |d| <= pi/4;
+// sin d and cos d are their Taylor series (coefficients 1/n!) to the terms d^9 and d^10,
+// whose truncation error at pi/4 is below 3e-9 relative.
+FOORT_HD void ff_sincos(float th_hi, float th_lo, float& s, float& c) {
+    constexpr float kPiO2Hi = 0x1.921fb6p+0f;    // pi/2 = hi + mid + lo to 2^-76
+    constexpr float kPiO2Mid = -0x1.777a5cp-25f;
+    constexpr float kPiO2Lo = -0x1.ee59dap-50f;
+    const float k = rintf(th_hi * 0.636619772f);
+    // th_hi - k hi is exact for |k| <= 2 (Sterbenz) and rounded once beyond; when it is 0
+    // the fma leaves d with one rounding relative to itself.
+    float d = fmaf(-k, kPiO2Hi, th_hi) + fmaf(-k, kPiO2Mid, th_lo);
+    d = fmaf(-k, kPiO2Lo, d);
+    const float d2 = d * d;
+    float sp = fmaf(d2, 2.75573192e-6f, -1.98412698e-4f);  // 1/9!, -1/7!
+    sp = fmaf(d2, sp, 8.33333333e-3f);                      // 1/5!
+    sp = fmaf(d2, sp, -1.66666667e-1f);                     // -1/3!
+    const float sd = fmaf(d * d2, sp, d);
+    float cp = fmaf(d2, -2.75573192e-7f, 2.48015873e-5f);   // -1/10!, 1/8!
+    cp = fmaf(d2, cp, -1.38888889e-3f);                     // -1/6!
+    cp = fmaf(d2, cp, 4.16666667e-2f);                      // 1/4!
+    cp = fmaf(d2, cp, -0.5f);                               // -1/2!
+    const float cd = fmaf(d2, cp, 1.0f);
+    const int q = static_cast<int>(k) & 3;
+    s = (q == 0) ? sd : (q == 1) ? cd : (q == 2) ? -sd : -cd;
+    c = (q == 0) ? cd : (q == 1) ? -sd : (q == 2) ? -cd : sd;
+}
+
 template <int MID>
 struct MixedMetric {
     static constexpr bool kAvailable = false;
@@ -87,6 +119,26 @@ FOORT_HD void accel_lagrange(const G5T<T>& d1, const G5T<T>& d2, const G5T<T>& g
     a[3] = T(-0.5) * (gu.tp * Ft + gu.pp * Fp);
     a[1] = T(-0.5) * gu.rr * Fr;
     a[2] = T(-0.5) * gu.hh * Fh;
+}
+
+// The acceleration in log-r mode (x1 = ln r). There d_x1 g_11 = 2 r^2 g_rr + r^3 d_r g_rr,
+// and its first part contributes -1/2 g^11 (2 r^2 g_rr) (u^1)^2 = -(u^1)^2 to a^1 exactly:
+// a pure coordinate term, at r = 1000 a thousand times the physical rest of a^1. It is
+// added as -(u^1)^2 rather than through g^rr g_rr, which in FP32 differs from 1 by a
+// few 1e-7: that would put a few 1e-7 of relative error on the dominant term of every
+// step's radial acceleration.
+template <typename T>
+FOORT_HD void accel_log_r(T r, G5T<T>& dr, G5T<T>& dh, G5T<T>& gu, const T u[4], T a[4]) {
+    const T r2 = r * r;
+    dr.tt *= r;
+    dr.tp *= r;
+    dr.hh *= r;
+    dr.pp *= r;
+    dr.rr *= r2 * r;  // r^3 d_r g_rr: the physical part of d_x1 g_11
+    dh.rr *= r2;
+    gu.rr /= r2;
+    accel_lagrange(dr, dh, gu, u, a);
+    a[1] -= u[1] * u[1];
 }
 
 }  // namespace foort

@@ -66,11 +66,11 @@ __host__ __device__ inline void ff_split(double d, float& hi, float& lo) {
 }
 __device__ __forceinline__ ff ff_of(const float* p) { return {p[0], p[1]}; }
 
-// Right-hand side at (x1, theta) with velocity u. `x1` is the compensated radial
-// coordinate (r, or ln r in log-r mode); r_+ / r_- (and their logarithms) come from the
-// image constants so that dp = r - r_+ and dm = r - r_- are accurate near the horizon.
+// Right-hand side at (x1, theta) with velocity u. `x1` and `th` are the compensated
+// coordinates (x1 = r, or ln r in log-r mode); r_+ / r_- (and their logarithms) come from
+// the image constants so that dp = r - r_+ and dm = r - r_- are accurate near the horizon.
 template <int MID, typename T>
-__device__ __forceinline__ void rhs_analytic(const T* q, const MixedConst& mc, bool rlog, ff x1, T th, const T u[4],
+__device__ __forceinline__ void rhs_analytic(const T* q, const MixedConst& mc, bool rlog, ff x1, ff th, const T u[4],
                                              T a[4]) {
     T r, dp, dm;
     if (!rlog) {
@@ -78,28 +78,55 @@ __device__ __forceinline__ void rhs_analytic(const T* q, const MixedConst& mc, b
         dp = T(__fsub_rn(x1.hi, mc.rp[0])) + (T(x1.lo) - T(mc.rp[1]));
         dm = T(__fsub_rn(x1.hi, mc.rm[0])) + (T(x1.lo) - T(mc.rm[1]));
     } else {
-        const T u1 = T(x1.hi) + T(x1.lo);
-        r = exp(u1);
-        dp = T(mc.rpv) * expm1((T(x1.hi) - T(mc.lrp[0])) + (T(x1.lo) - T(mc.lrp[1])));
-        dm = (mc.rmv > 0.0) ? T(mc.rmv) * expm1((T(x1.hi) - T(mc.lrm[0])) + (T(x1.lo) - T(mc.lrm[1]))) : r;
+        // exp(hi + lo) = exp(hi) (1 + lo): rounding ln r (up to 7 at r = 1000) to one
+        // float first would cost 2.4e-7 of relative accuracy in r
+        const T yp = (T(x1.hi) - T(mc.lrp[0])) + (T(x1.lo) - T(mc.lrp[1]));  // ln(r / r_+)
+        if constexpr (sizeof(T) == sizeof(float)) {
+            const float e = expf(x1.hi);
+            r = fmaf(e, x1.lo, e);
+            // r - r_+ from expm1 only where it cancels (r < e r_+): beyond, the float
+            // argument's rounding (2.4e-7 at ln(r / r_+) = 6) would enter Delta and g_rr
+            // as a relative error of that size. r - r_- never cancels (r >= r_+ > r_-).
+            dp = (yp > 1.f) ? r - mc.rp[0] : mc.rp[0] * expm1f(yp);
+            dm = r - mc.rm[0];
+        } else {
+            r = exp(T(x1.hi) + T(x1.lo));
+            dp = T(mc.rpv) * expm1(yp);
+            dm = (mc.rmv > 0.0) ? T(mc.rmv) * expm1((T(x1.hi) - T(mc.lrm[0])) + (T(x1.lo) - T(mc.lrm[1]))) : r;
+        }
     }
     T s, c;
-    sincos(th, &s, &c);
+    if constexpr (sizeof(T) == sizeof(float)) {
+        ff_sincos(th.hi, th.lo, s, c);
+    } else {
+        sincos(T(th.hi) + T(th.lo), &s, &c);
+    }
     G5T<T> dr, dh, gu;
     T grr;
     MixedMetric<MID>::template eval<T>(q, r, dp, dm, s, c, dr, dh, gu, grr);
-    if (rlog) to_log_r(r, grr, dr, dh, gu);
-    accel_lagrange(dr, dh, gu, u, a);
+    if (rlog) {
+        accel_log_r(r, dr, dh, gu, u, a);
+    } else {
+        accel_lagrange(dr, dh, gu, u, a);
+    }
 }
 
+// The called form of the FP32 right-hand side. Velocity and acceleration travel by value
+// so that the call passes them in registers (arrays would go through the stack: a local
+// store and load on the critical path of every evaluation; 7 % of a C2 launch).
+struct F4 {
+    float x, y, z, w;
+};
 template <int MID>
-__device__ __noinline__ void rhs_f32_called(const float* q, const MixedConst& mc, bool rlog, ff x1, float th,
-                                            const float u[4], float a[4]) {
+__device__ __noinline__ F4 rhs_f32_called(const float* q, const MixedConst& mc, bool rlog, ff x1, ff th, F4 uv) {
+    const float u[4] = {uv.x, uv.y, uv.z, uv.w};
+    float a[4];
     rhs_analytic<MID, float>(q, mc, rlog, x1, th, u, a);
+    return F4{a[0], a[1], a[2], a[3]};
 }
 
 template <int MID>
-__device__ __noinline__ void rhs_fp64_path(const double* q, const MixedConst& mc, bool rlog, ff x1, double th,
+__device__ __noinline__ void rhs_fp64_path(const double* q, const MixedConst& mc, bool rlog, ff x1, ff th,
                                            const float uf[4], float a[4]) {
     double u[4] = {uf[0], uf[1], uf[2], uf[3]}, ad[4];
     rhs_analytic<MID, double>(q, mc, rlog, x1, th, u, ad);
@@ -111,10 +138,12 @@ __device__ __noinline__ void rhs_fp64_path(const double* q, const MixedConst& mc
 // which is the reference's expression with eps factored out, evaluated with correctly
 // rounded operations and eps carried as a float-float pair: the step size then has no
 // systematic bias against the FP64 kernel's (a bias would shift where along the ray
-// the last step lands).
-__device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const MixedConst& mc, float th, const float v[4]) {
-    const float pi = mc.pi[0];
-    const float m = (pi - th < th) ? pi - th : th;
+// the last step lands). pi - theta is formed in float-float: near the pole both round to
+// the same float, and a zero m would collapse the step to the smallest step size.
+__device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const MixedConst& mc, ff th, const float v[4]) {
+    const ff dpi = ff_add(ff_of(mc.pi), ff_neg(th));
+    const float t = ff_f(th), pt = ff_f(dpi);
+    const float m = (pt < t) ? pt : t;
     const float s1 = __fadd_rn(fabsf(v[1]), 1e-20f);
     const float s2 = __fdiv_rn(__fadd_rn(fabsf(v[2]), 1e-20f), fabsf(m));
     const float s3 = fabsf(__fadd_rn(v[3], 1e-20f));
@@ -250,16 +279,20 @@ struct MixedEngine {
         return FOORT_TERMCODE_CONTINUE;
     }
 
-    static __device__ __forceinline__ void rhs(const ImageConst& I, const RunConst& R, Lane& L, ff x1, float th,
+    static __device__ __forceinline__ void rhs(const ImageConst& I, const RunConst& R, Lane& L, ff x1, ff th,
                                                const float u[4], float a[4]) {
         const bool rlog = R.rlog != 0;
         if (I.mx.r_fp64 > 0.f && x1.hi < I.mx.r_fp64) {
-            rhs_fp64_path<MID>(I.m.q, I.mx, rlog, x1, static_cast<double>(th), u, a);
+            rhs_fp64_path<MID>(I.m.q, I.mx, rlog, x1, th, u, a);
             ++L.fp64;
         } else if (MixedMetric<MID>::kInline) {
             rhs_analytic<MID, float>(I.mx.q, I.mx, rlog, x1, th, u, a);
         } else {
-            rhs_f32_called<MID>(I.mx.q, I.mx, rlog, x1, th, u, a);
+            const F4 r = rhs_f32_called<MID>(I.mx.q, I.mx, rlog, x1, th, F4{u[0], u[1], u[2], u[3]});
+            a[0] = r.x;
+            a[1] = r.y;
+            a[2] = r.z;
+            a[3] = r.w;
         }
     }
 
@@ -267,23 +300,24 @@ struct MixedEngine {
         float uf[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) uf[i] = ff_f(L.v[i]);
-        const float th0 = ff_f(L.x[2]);
-        const float h = adaptive_step_f32(R, I.mx, th0, uf);
+        const float h = adaptive_step_f32(R, I.mx, L.x[2], uf);
         float du[4];
         float dxc[4];  // O(h^2) part of the position increment
         if (INTEG == FOORT_INTEGRATOR_RK4) {
             float k1[4], k2[4], k3[4], k4[4], us[4];
             const float hh = 0.5f * h;
-            rhs(I, R, L, L.x[1], th0, uf, k1);
+            rhs(I, R, L, L.x[1], L.x[2], uf, k1);
 #pragma unroll
             for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
-            rhs(I, R, L, ff_add_f(L.x[1], hh * uf[1]), th0 + hh * uf[2], us, k2);
+            rhs(I, R, L, ff_add_f(L.x[1], hh * uf[1]), ff_add_f(L.x[2], hh * uf[2]), us, k2);
 #pragma unroll
             for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
-            rhs(I, R, L, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])), th0 + hh * (uf[2] + hh * k1[2]), us, k3);
+            rhs(I, R, L, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])), ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2])),
+                us, k3);
 #pragma unroll
             for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
-            rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), th0 + h * (uf[2] + hh * k2[2]), us, k4);
+            rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])), us,
+                k4);
             // h / 6 is divided, not multiplied by a rounded 1/6: that constant is 3e-8 too
             // large, which would scale every velocity increment by the same factor and,
             // amplified by strongly bent orbits, bias the escape direction by ~1e-7.
@@ -298,7 +332,7 @@ struct MixedEngine {
             // velocity Verlet (Integrators.cpp:99-152); the velocity change of each
             // iteration is formed as h/2 (a1_new - a1_old), free of cancellation.
             float a0[4], a1[4], vi[4];
-            rhs(I, R, L, L.x[1], th0, uf, a0);
+            rhs(I, R, L, L.x[1], L.x[2], uf, a0);
             const float hh2 = 0.5f * h * h;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
@@ -306,7 +340,7 @@ struct MixedEngine {
                 vi[i] = uf[i] + h * a0[i];
             }
             const ff x1n = ff_add_f(ff_add(L.x[1], two_prod(h, L.v[1].hi)), __fmaf_rn(h, L.v[1].lo, dxc[1]));
-            const float thn = th0 + h * uf[2] + dxc[2];
+            const ff thn = ff_add_f(ff_add(L.x[2], two_prod(h, L.v[2].hi)), __fmaf_rn(h, L.v[2].lo, dxc[2]));
             rhs(I, R, L, x1n, thn, vi, a1);
             L.rhs += 2;
             const float h2 = 0.5f * h;

@@ -54,14 +54,19 @@ void run(const char* name, const double* params, bool rlog) {
         accel_lagrange(dr, dh, gu, u, ad);
         // float path
         float rf = static_cast<float>(r), dpf = static_cast<float>(r - rp), dmf = static_cast<float>(r - rm);
-        float sf = std::sin(static_cast<float>(th)), cf = std::cos(static_cast<float>(th));
+        float sf, cf;  // as the kernel forms them, from the float-float angle
+        const float th_hi = static_cast<float>(th);
+        ff_sincos(th_hi, static_cast<float>(th - th_hi), sf, cf);
         G5T<float> fr, fh, fu;
         float frr;
         MixedMetric<MID>::template eval<float>(qf, rf, dpf, dmf, sf, cf, fr, fh, fu, frr);
-        if (rlog) to_log_r(rf, frr, fr, fh, fu);
         float uf[4] = {static_cast<float>(u[0]), static_cast<float>(u[1]), static_cast<float>(u[2]), static_cast<float>(u[3])};
         float af[4];
-        accel_lagrange(fr, fh, fu, uf, af);
+        if (rlog) {
+            accel_log_r(rf, fr, fh, fu, uf, af);  // the kernel's log-r form
+        } else {
+            accel_lagrange(fr, fh, fu, uf, af);
+        }
         double scale = 0, diff = 0;
         for (int i = 0; i < 4; ++i) {
             scale = std::max(scale, std::fabs(ad[i]));
@@ -75,7 +80,39 @@ void run(const char* name, const double* params, bool rlog) {
     std::printf("%s %.3e %.3e %.3e %.3e\n", name, q(0.5), q(0.9), q(0.99), errs.back());
 }
 
+// ff_sincos against long-double sin and cos of the exact float-float angle: relative
+// error max(|ds| / |s|, |dc| / |c|), on angles across (-0.5, pi + 0.5) and within 1e-12 to
+// 1e-3 of 0, pi/2 and pi, where the small one of sin and cos must stay accurate.
+void sincos_check() {
+    std::mt19937_64 rng(3);
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    const long double kPi = 3.141592653589793238462643383279503L;
+    std::vector<double> errs;
+    for (int k = 0; k < 200000; ++k) {
+        long double th;
+        const int kind = k % 4;
+        if (kind == 0) {
+            th = -0.5L + (kPi + 1.0L) * U(rng);
+        } else {
+            const long double off = std::pow(10.0L, -12.0L + 9.0L * U(rng)) * (U(rng) < 0.5 ? -1 : 1);
+            th = (kind == 1 ? 0.0L : kind == 2 ? kPi / 2 : kPi) + off;
+        }
+        const float hi = static_cast<float>(th);
+        const float lo = static_cast<float>(th - hi);
+        const long double te = static_cast<long double>(hi) + lo;
+        float s, c;
+        ff_sincos(hi, lo, s, c);
+        const long double se = std::sin(te), ce = std::cos(te);
+        const double e = std::max(std::fabs((s - se) / se), std::fabs((c - ce) / ce));
+        errs.push_back(std::isfinite(e) ? e : 1e30);
+    }
+    std::sort(errs.begin(), errs.end());
+    auto q = [&](double f) { return errs[static_cast<size_t>(f * (errs.size() - 1))]; };
+    std::printf("ff_sincos %.3e %.3e %.3e %.3e\n", q(0.5), q(0.9), q(0.99), errs.back());
+}
+
 int main() {
+    sincos_check();
     const double kerr99[6] = {0.99}, kerr5[6] = {0.5}, kerr998[6] = {0.998};
     const double joh_c4[6] = {0.9, -0.5, 0, 0, 0}, joh_test[6] = {0.7, 2.0, 0, 0, 0}, joh_all[6] = {0.8, 1.0, 0.5, 0.2, 0.1};
     const double none[6] = {0};

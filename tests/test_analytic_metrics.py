@@ -55,3 +55,6 @@ def test_fp32_acceleration_accuracy(tmp_path):
         print(line)
         # FP32 has 6e-8 unit roundoff; a few operations deep the acceleration keeps ~1e-7
         assert p50 < 3e-7 and p99 < 3e-6 and mx < 1e-4, line
+        if name == "ff_sincos":
+            # the mixed kernel's sin/cos: a few roundings, relative, also next to the poles
+            assert mx < 5e-7, line
