@@ -48,8 +48,7 @@ SINCOS_PER_STEP = {("kerr", "rk4"): 20, ("johannsen", "rk4"): 20, ("johannsen", 
 OPS_PER_EXTRA_VERLET_RHS = 380
 
 
-def dist_env():
-    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+from foort_gb300.multirank import dist_env  # noqa: E402
 
 
 def log(*a):
@@ -313,7 +312,7 @@ def main():
 
     import torch
     import foort_gb300
-    from foort_gb300 import abi
+    from foort_gb300 import abi, multirank
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -326,11 +325,7 @@ def main():
         torch.cuda.synchronize()
 
     def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return multirank.max_over_ranks(x, dist, device="cuda")
 
     # ---- prepare: the workload's pixel lists (one adaptive run with the mixed kernel)
     wl = workload(args.workload, abi.PREC_MIXED, args.iteration_pixels)
