@@ -160,17 +160,24 @@ def emit(name, gdd, guu, dl, inv=False):
     exprs.append(cond(gdd["rr"], dl))
     names.append("grr")
     repl, red = sp.cse(exprs, symbols=sp.numbered_symbols("t"), optimizations="basic")
-    lines = ["const T u = T(1) / r;"] if inv else []
+    lines = ["const T u = rcp(r);"] if inv else []
+    # common subexpressions that are powers of u: their negative powers are powers of r
+    upow = {sym: int(e.exp) for sym, e in repl if isinstance(e, sp.Pow) and e.base == u and e.exp.is_Integer}
+    upow.update({sym: 1 for sym, e in repl if e == u})
     for sym, e in repl:
-        lines.append(f"const T {sym} = {ccode(e)};")
+        lines.append(f"const T {sym} = {ccode(e, upow)};")
     for n, e in zip(names, red):
-        lines.append(f"{n} = {ccode(e)};")
+        lines.append(f"{n} = {ccode(e, upow)};")
     return "\n".join(lines)
 
 
-def ccode(e):
+def ccode(e, upow=None):
     """C++ for e with every constant and operation in the template type T: integer powers
-    become products, negative powers divisions."""
+    become products, negative powers of u = 1/r powers of r, other negative powers
+    divisions."""
+    r_sym = sp.Symbol("r")
+    upow = dict(upow or {})
+    upow[u] = 1
 
     def atom(x):
         if isinstance(x, sp.Symbol):
@@ -205,7 +212,9 @@ def ccode(e):
         if isinstance(x, sp.Mul):
             num, den = [], []
             for f in x.args:
-                if isinstance(f, sp.Pow) and f.exp.is_Integer and f.exp < 0:
+                if isinstance(f, sp.Pow) and f.exp.is_Integer and f.exp < 0 and f.base in upow:
+                    num.append(pw(r_sym, -int(f.exp) * upow[f.base]))
+                elif isinstance(f, sp.Pow) and f.exp.is_Integer and f.exp < 0:
                     den.append(pw(f.base, -int(f.exp)))
                 elif isinstance(f, sp.Rational) and not isinstance(f, sp.Integer) and f.p in (1, -1):
                     num.append("T(-1)" if f.p < 0 else "T(1)")
@@ -223,6 +232,8 @@ def ccode(e):
                 n = int(x.exp)
                 if n > 0:
                     return pw(x.base, n)
+                if x.base in upow:
+                    return pw(r_sym, -n * upow[x.base])
                 return f"(T(1)/{pw(x.base, -n)})"
             raise RuntimeError(f"non-integer power: {x}")
         raise RuntimeError(f"cannot print {type(x)}: {x}")
