@@ -77,9 +77,9 @@ struct MixedMetric {
 };
 
 // kInline: inline the body into each RK4 stage, or call it. Calling keeps large bodies
-// (Johannsen, ~300 temporaries) out of the register allocation of the stepping loop,
-// and for Kerr it measured 7 % faster on GB300: four inlined copies overflow the
-// instruction cache of a lone warp (C2, 5 rounds: 1.33 s called vs 1.43 s inlined).
+// (Johannsen, ~300 temporaries) out of the register allocation of the stepping loop.
+// Kerr is inlined: with branch-free reciprocals its four copies fit the instruction
+// cache, and C2's five rounds take 695 ms inlined against 786 ms called on GB300.
 #define FOORT_DEFINE_MIXED_METRIC(ID, BODY, INL)                                                   \
     template <>                                                                                    \
     struct MixedMetric<ID> {                                                                       \
@@ -93,7 +93,7 @@ struct MixedMetric {
         }                                                                                          \
     };
 
-FOORT_DEFINE_MIXED_METRIC(kKerr, FOORT_MIXED_BODY_KERR, false)
+FOORT_DEFINE_MIXED_METRIC(kKerr, FOORT_MIXED_BODY_KERR, true)
 FOORT_DEFINE_MIXED_METRIC(kJohannsen, FOORT_MIXED_BODY_JOHANNSEN, false)
 FOORT_DEFINE_MIXED_METRIC(kFlat, FOORT_MIXED_BODY_FLAT, true)
 

@@ -145,9 +145,9 @@ __device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const Mixe
     const float t = ff_f(th), pt = ff_f(dpi);
     const float m = (pt < t) ? pt : t;
     const float s1 = __fadd_rn(fabsf(v[1]), 1e-20f);
-    const float s2 = __fdiv_rn(__fadd_rn(fabsf(v[2]), 1e-20f), fabsf(m));
+    const float s2 = __fmul_rn(__fadd_rn(fabsf(v[2]), 1e-20f), rcp(fabsf(m)));
     const float s3 = fabsf(__fadd_rn(v[3], 1e-20f));
-    const float inv = __frcp_rn(__fadd_rn(__fadd_rn(s1, s2), s3));
+    const float inv = rcp(__fadd_rn(__fadd_rn(s1, s2), s3));
     const float h = __fmaf_rn(mc.eps[0], inv, __fmul_rn(mc.eps[1], inv));
     const float hmin = mc.hmin;
     return (h < hmin) ? hmin : h;
@@ -318,10 +318,13 @@ struct MixedEngine {
             for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
             rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])), us,
                 k4);
-            // h / 6 is divided, not multiplied by a rounded 1/6: that constant is 3e-8 too
-            // large, which would scale every velocity increment by the same factor and,
-            // amplified by strongly bent orbits, bias the escape direction by ~1e-7.
-            const float h6 = __fdiv_rn(h, 6.f), hh6 = __fmul_rn(h, h6);
+            // h / 6 is a quotient, not a product with a rounded 1/6: that constant is 3e-8
+            // too large, which would scale every velocity increment by the same factor
+            // and, amplified by strongly bent orbits, bias the escape direction by ~1e-7.
+            // One Newton-Raphson correction of h * (1/6) gives the quotient to within an
+            // ulp without that bias: q1 = q0 + (h - 6 q0) / 6.
+            const float q0 = __fmul_rn(h, 0.166666672f);
+            const float h6 = __fmaf_rn(__fmaf_rn(-6.f, q0, h), 0.166666672f, q0), hh6 = __fmul_rn(h, h6);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 du[i] = h6 * (k1[i] + 2.f * k2[i] + 2.f * k3[i] + k4[i]);
@@ -360,7 +363,7 @@ struct MixedEngine {
                         num += dv[i] * dv[i];
                         den += nvi * nvi;
                     }
-                    if (!(num / den > tol2)) break;
+                    if (!(num > tol2 * den)) break;  // num / den > tol2 with den = |v|^2 > 0
                     if (it >= R.verlet_cap) {
                         L.err |= FOORT_ERR_VERLET_ITER;
                         break;
@@ -379,12 +382,13 @@ struct MixedEngine {
                 }
             }
         }
-        // x += h u + dxc;  u += du;  lambda += h  (compensated)
+        // x += h u + dxc;  u += du;  lambda += h  (compensated). The increments are
+        // rounded to one float each (relative error 6e-8 of a step's change, unbiased,
+        // so it accumulates as a random walk); what the float-float sum prevents is the
+        // absorption of small increments into the large coordinate.
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            ff hu = two_prod(h, L.v[i].hi);
-            hu.lo = __fmaf_rn(h, L.v[i].lo, hu.lo) + dxc[i];
-            L.x[i] = ff_add(L.x[i], hu);
+            L.x[i] = ff_add_f(L.x[i], __fmaf_rn(h, L.v[i].hi, dxc[i]));
             L.v[i] = ff_add_f(L.v[i], du[i]);
         }
         L.lam = ff_add_f(L.lam, h);
