@@ -136,7 +136,7 @@ FOORT_HD void accel_lagrange(const G5T<T>& d1, const G5T<T>& d2, const G5T<T>& g
 // few 1e-7: that would put a few 1e-7 of relative error on the dominant term of every
 // step's radial acceleration.
 template <typename T>
-FOORT_HD void accel_log_r(T r, G5T<T>& dr, G5T<T>& dh, G5T<T>& gu, const T u[4], T a[4]) {
+FOORT_HD void scale_log_r(T r, G5T<T>& dr, G5T<T>& dh, G5T<T>& gu) {
     const T r2 = r * r;
     dr.tt *= r;
     dr.tp *= r;
@@ -145,6 +145,10 @@ FOORT_HD void accel_log_r(T r, G5T<T>& dr, G5T<T>& dh, G5T<T>& gu, const T u[4],
     dr.rr *= r2 * r;  // r^3 d_r g_rr: the physical part of d_x1 g_11
     dh.rr *= r2;
     gu.rr /= r2;
+}
+template <typename T>
+FOORT_HD void accel_log_r(T r, G5T<T>& dr, G5T<T>& dh, G5T<T>& gu, const T u[4], T a[4]) {
+    scale_log_r(r, dr, dh, gu);
     accel_lagrange(dr, dh, gu, u, a);
     a[1] -= u[1] * u[1];
 }

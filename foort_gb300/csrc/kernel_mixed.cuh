@@ -66,12 +66,20 @@ __host__ __device__ inline void ff_split(double d, float& hi, float& lo) {
 }
 __device__ __forceinline__ ff ff_of(const float* p) { return {p[0], p[1]}; }
 
-// Right-hand side at (x1, theta) with velocity u. `x1` and `th` are the compensated
-// coordinates (x1 = r, or ln r in log-r mode); r_+ / r_- (and their logarithms) come from
-// the image constants so that dp = r - r_+ and dm = r - r_- are accurate near the horizon.
+// The right-hand side in two parts: the metric part depends on the position only (the
+// expensive part: angle, metric derivatives, inverse metric), the contraction with the
+// velocity is cheap. Splitting them lets RK4 evaluate the metric at the next stage's
+// position while the current stage's contraction waits for its velocity.
+template <typename T>
+struct MetricAt {
+    G5T<T> d1, d2, gu;  // d_x1 g, d_theta g (scaled to x1 = ln r in log-r mode), g^uu
+};
+
+// Metric part at (x1, theta). `x1` and `th` are the compensated coordinates (x1 = r, or
+// ln r in log-r mode); r_+ / r_- (and their logarithms) come from the image constants so
+// that dp = r - r_+ and dm = r - r_- are accurate near the horizon.
 template <int MID, typename T>
-__device__ __forceinline__ void rhs_analytic(const T* q, const MixedConst& mc, bool rlog, ff x1, ff th, const T u[4],
-                                             T a[4]) {
+__device__ __forceinline__ MetricAt<T> metric_part(const T* q, const MixedConst& mc, bool rlog, ff x1, ff th) {
     T r, dp, dm;
     if (!rlog) {
         r = T(x1.hi) + T(x1.lo);
@@ -101,14 +109,26 @@ __device__ __forceinline__ void rhs_analytic(const T* q, const MixedConst& mc, b
     } else {
         sincos(T(th.hi) + T(th.lo), &s, &c);
     }
-    G5T<T> dr, dh, gu;
+    MetricAt<T> m;
     T grr;
-    MixedMetric<MID>::template eval<T>(q, r, dp, dm, s, c, dr, dh, gu, grr);
-    if (rlog) {
-        accel_log_r(r, dr, dh, gu, u, a);
-    } else {
-        accel_lagrange(dr, dh, gu, u, a);
-    }
+    MixedMetric<MID>::template eval<T>(q, r, dp, dm, s, c, m.d1, m.d2, m.gu, grr);
+    if (rlog) scale_log_r(r, m.d1, m.d2, m.gu);
+    return m;
+}
+
+// Contraction with the velocity (accel_lagrange; in log-r mode plus the exact coordinate
+// term -(u^1)^2 of accel_log_r).
+template <typename T>
+__device__ __forceinline__ void accel_part(const MetricAt<T>& m, bool rlog, const T u[4], T a[4]) {
+    accel_lagrange(m.d1, m.d2, m.gu, u, a);
+    if (rlog) a[1] -= u[1] * u[1];
+}
+
+// Right-hand side at (x1, theta) with velocity u.
+template <int MID, typename T>
+__device__ __forceinline__ void rhs_analytic(const T* q, const MixedConst& mc, bool rlog, ff x1, ff th, const T u[4],
+                                             T a[4]) {
+    accel_part(metric_part<MID, T>(q, mc, rlog, x1, th), rlog, u, a);
 }
 
 // The called form of the FP32 right-hand side. Velocity and acceleration travel by value
@@ -306,18 +326,47 @@ struct MixedEngine {
         if (INTEG == FOORT_INTEGRATOR_RK4) {
             float k1[4], k2[4], k3[4], k4[4], us[4];
             const float hh = 0.5f * h;
-            rhs(I, R, L, L.x[1], L.x[2], uf, k1);
+            if (MixedMetric<MID>::kInline && !(I.mx.r_fp64 > 0.f)) {
+                // The stage positions need only the velocities of earlier stages: x + h/2 u
+                // (stage 2) none, x + h/2 (u + h/2 k1) (stage 3) k1, x + h (u + h/2 k2)
+                // (stage 4) k2. So the metric part of stage 2 runs beside stage 1's, and
+                // those of stages 3 and 4 beside the contractions of stages 2 and 3: the
+                // dependent chain of a step is two metric evaluations and three
+                // contractions instead of four of each. Same operations, same results.
+                const bool rlog = R.rlog != 0;
+                const MetricAt<float> m1 = metric_part<MID, float>(I.mx.q, I.mx, rlog, L.x[1], L.x[2]);
+                const MetricAt<float> m2 = metric_part<MID, float>(I.mx.q, I.mx, rlog, ff_add_f(L.x[1], hh * uf[1]),
+                                                                   ff_add_f(L.x[2], hh * uf[2]));
+                accel_part(m1, rlog, uf, k1);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
-            rhs(I, R, L, ff_add_f(L.x[1], hh * uf[1]), ff_add_f(L.x[2], hh * uf[2]), us, k2);
+                for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
+                const MetricAt<float> m3 = metric_part<MID, float>(
+                    I.mx.q, I.mx, rlog, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])),
+                    ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2])));
+                accel_part(m2, rlog, us, k2);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
-            rhs(I, R, L, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])), ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2])),
-                us, k3);
+                for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
+                const MetricAt<float> m4 = metric_part<MID, float>(
+                    I.mx.q, I.mx, rlog, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])),
+                    ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])));
+                accel_part(m3, rlog, us, k3);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
-            rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])), us,
-                k4);
+                for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
+                accel_part(m4, rlog, us, k4);
+            } else {
+                rhs(I, R, L, L.x[1], L.x[2], uf, k1);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
+                rhs(I, R, L, ff_add_f(L.x[1], hh * uf[1]), ff_add_f(L.x[2], hh * uf[2]), us, k2);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
+                rhs(I, R, L, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])), ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2])),
+                    us, k3);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
+                rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])),
+                    us, k4);
+            }
             // h / 6 is a quotient, not a product with a rounded 1/6: that constant is 3e-8
             // too large, which would scale every velocity increment by the same factor
             // and, amplified by strongly bent orbits, bias the escape direction by ~1e-7.
