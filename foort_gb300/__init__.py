@@ -43,6 +43,7 @@ def load():
     lib.foort_gpu_set_budget.argtypes = [vp, u64]
     lib.foort_gpu_cancel.argtypes = [vp]
     lib.foort_gpu_set_launch.argtypes = [vp, u32, u32]
+    lib.foort_gpu_set_lanes.argtypes = [vp, u32]
     lib.foort_gpu_get_stats.argtypes = [vp, C.POINTER(abi.Stats)]
     lib.foort_gpu_destroy.argtypes = [vp]
     lib.foort_gpu_destroy.restype = None
@@ -146,6 +147,10 @@ class Engine:
 
     def set_launch(self, block_size=0, blocks_per_sm=0):
         self._check(self._lib.foort_gpu_set_launch(self._ctx, block_size, blocks_per_sm))
+
+    def set_lanes(self, lanes_per_geodesic=0):
+        """0: chosen per launch; 1 or 2 lanes per geodesic where the kernel has both."""
+        self._check(self._lib.foort_gpu_set_lanes(self._ctx, lanes_per_geodesic))
 
     def stats(self):
         s = abi.Stats()

@@ -145,7 +145,7 @@ class Stats(C.Structure):
         ("status", C.c_uint32),
         ("n_blocks", C.c_uint32),
         ("block_size", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("lanes_per_geodesic", C.c_uint32),
     ]
 
 

@@ -37,6 +37,7 @@ struct foort_ctx {
     uint64_t budget = 0;
     uint64_t last_n = 0;
     uint32_t block_size = 0, blocks_per_sm = 0;
+    uint32_t lanes = 0;  // lanes per geodesic: 0 chosen per launch, 1, 2
     int device = 0, num_sms = 0;
     bool pending = false;
     foort_stats stats{};
@@ -200,6 +201,57 @@ const void* select_kernel(const RunConst& R) {
     return fp64_kernel(R.metric_id, R.integrator);
 }
 
+// The two-lanes-per-geodesic kernel for these options, or nullptr (FP64, Verlet, the
+// called plugins, the FP64 right-hand side near the horizon).
+const void* select_pair_kernel(const RunConst& R) {
+    if (R.precision != FOORT_PREC_MIXED || R.mixed_fp64_margin > 0.0) return nullptr;
+    return mixed_pair_kernel_variant(R.metric_id, R.integrator, (R.mixed_options & FOORT_MIXED_FP64_DECISIONS) != 0);
+}
+
+struct LaunchShape {
+    const void* fn = nullptr;
+    uint32_t grid = 0, block = 0, lanes = 1;
+};
+
+// Kernel and grid of a launch of n geodesics: a persistent grid of at most the resident
+// CTAs. lanes_pref 0 chooses two lanes per geodesic where that kernel exists and all n
+// geodesics fit on the GPU's resident lanes that way (then a step's latency, not the
+// GPU's throughput, sets the pace, and two lanes halve the metric work on it); 1 and 2
+// force one or two lanes where possible.
+int choose_launch(foort_ctx* ctx, const RunConst& R, uint64_t n, int num_sms, uint32_t block_size,
+                  uint32_t blocks_per_sm, uint32_t lanes_pref, LaunchShape& out) {
+    const uint32_t bs = block_size ? block_size : 128;
+    auto resident = [&](const void* fn, int& per_sm) -> int {
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, static_cast<int>(bs), 0));
+        if (blocks_per_sm) per_sm = std::min<int>(per_sm, static_cast<int>(blocks_per_sm));
+        return FOORT_OK;
+    };
+    const void* fn = select_kernel(R);
+    if (!fn) return fail(ctx, FOORT_E_UNSUPPORTED, "no kernel for this metric / integrator / precision");
+    int per_sm = 0, rc = 0;
+    uint32_t lanes = 1;
+    const void* fn2 = (lanes_pref != 1) ? select_pair_kernel(R) : nullptr;
+    if (fn2) {
+        int per_sm2 = 0;
+        if ((rc = resident(fn2, per_sm2))) return rc;
+        const uint64_t cap2 = static_cast<uint64_t>(per_sm2) * static_cast<uint64_t>(num_sms) * bs;
+        if (per_sm2 > 0 && (lanes_pref == 2 || 2 * n <= cap2)) {
+            fn = fn2;
+            per_sm = per_sm2;
+            lanes = 2;
+        }
+    }
+    if (lanes == 1 && (rc = resident(fn, per_sm))) return rc;
+    if (per_sm <= 0) return fail(ctx, FOORT_E_CUDA, "kernel does not fit on an SM with this block size");
+    const uint64_t full = static_cast<uint64_t>(per_sm) * static_cast<uint64_t>(num_sms);
+    const uint64_t need = (lanes * n + bs - 1) / bs;
+    out.fn = fn;
+    out.grid = static_cast<uint32_t>(std::max<uint64_t>(1, std::min(full, need)));
+    out.block = bs;
+    out.lanes = lanes;
+    return FOORT_OK;
+}
+
 int ensure_capacity(foort_ctx* ctx, uint64_t n) {
     if (n <= ctx->cap) return FOORT_OK;
     if (ctx->d_px) cudaFree(ctx->d_px);
@@ -214,16 +266,11 @@ int ensure_capacity(foort_ctx* ctx, uint64_t n) {
 }
 
 int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, cudaStream_t st) {
-    const void* fn = select_kernel(ctx->rc);
-    if (!fn) return fail(ctx, FOORT_E_UNSUPPORTED, "no kernel for this metric / integrator / precision");
-    uint32_t bs = ctx->block_size ? ctx->block_size : 128;
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, static_cast<int>(bs), 0));
-    if (per_sm <= 0) return fail(ctx, FOORT_E_CUDA, "kernel does not fit on an SM with this block size");
-    if (ctx->blocks_per_sm) per_sm = std::min<int>(per_sm, static_cast<int>(ctx->blocks_per_sm));
-    uint64_t full = static_cast<uint64_t>(per_sm) * static_cast<uint64_t>(ctx->num_sms);
-    uint64_t need = (n + bs - 1) / bs;
-    uint32_t grid = static_cast<uint32_t>(std::max<uint64_t>(1, std::min(full, need)));
+    LaunchShape ls;
+    int rc = choose_launch(ctx, ctx->rc, n, ctx->num_sms, ctx->block_size, ctx->blocks_per_sm, ctx->lanes, ls);
+    if (rc) return rc;
+    const void* fn = ls.fn;
+    const uint32_t bs = ls.block, grid = ls.grid;
     *ctx->h_cancel = 0;
     CK(cudaMemsetAsync(ctx->d_ctr, 0, kNumCtr * sizeof(unsigned long long), st));
     LaunchArgs A{};
@@ -248,6 +295,7 @@ int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_
     CK(cudaMemcpyAsync(ctx->h_ctr, ctx->d_ctr, kNumCtr * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     ctx->stats.n_blocks = grid;
     ctx->stats.block_size = bs;
+    ctx->stats.lanes_per_geodesic = ls.lanes;
     ctx->last_n = n;
     ctx->last_stream = st;
     ctx->pending = true;
@@ -402,6 +450,13 @@ int foort_gpu_set_launch(foort_ctx* ctx, uint32_t block_size, uint32_t blocks_pe
         return fail(ctx, FOORT_E_BADARG, "block_size must be a multiple of 32 and at most 128");
     ctx->block_size = block_size;
     ctx->blocks_per_sm = blocks_per_sm;
+    return FOORT_OK;
+}
+
+int foort_gpu_set_lanes(foort_ctx* ctx, uint32_t lanes_per_geodesic) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    if (lanes_per_geodesic > 2) return fail(ctx, FOORT_E_BADARG, "lanes_per_geodesic must be 0 (automatic), 1 or 2");
+    ctx->lanes = lanes_per_geodesic;
     return FOORT_OK;
 }
 
@@ -567,13 +622,10 @@ extern "C" int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foo
     }
     CK(cudaMemsetAsync(d_ctr, 0, kNumCtr * sizeof(unsigned long long), st));
 
-    const uint32_t bs = 128;
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, static_cast<int>(bs), 0));
-    if (per_sm <= 0) return fail(nullptr, FOORT_E_CUDA, "kernel does not fit on an SM with this block size");
-    const uint64_t full = static_cast<uint64_t>(per_sm) * static_cast<uint64_t>(nd.num_sms);
-    const uint64_t need = (n + bs - 1) / bs;
-    const uint32_t grid = static_cast<uint32_t>(std::max<uint64_t>(1, std::min(full, need)));
+    LaunchShape ls;
+    if ((rc = choose_launch(nullptr, R0, n, nd.num_sms, 0, 0, 0, ls))) return rc;
+    const uint32_t bs = ls.block, grid = ls.grid;
+    fn = ls.fn;
     LaunchArgs A{};
     A.px = d_px;
     A.out = d_out;
@@ -599,6 +651,7 @@ extern "C" int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foo
     stats->fp64_steps = h_ctr[kCtrFp64Steps];
     stats->n_blocks = grid;
     stats->block_size = bs;
+    stats->lanes_per_geodesic = ls.lanes;
     rc = FOORT_OK;
     if (h_ctr[kCtrStatus] & kStatusBudget)
         rc = fail(nullptr, FOORT_E_BUDGET, "global step budget exhausted; unfinished geodesics are marked");

@@ -10,12 +10,25 @@ __global__ void __launch_bounds__(128) integrate_mixed_kernel(const __grid_const
     persistent_loop<MixedEngine<MID, INTEG, D64>>(A, R);
 }
 
+// Two lanes per geodesic (RK4): for launches with fewer geodesics than the GPU has lanes.
+template <int MID, bool D64>
+__global__ void __launch_bounds__(128) integrate_mixed_pair_kernel(const __grid_constant__ LaunchArgs A,
+                                                                   const __grid_constant__ RunConst R) {
+    persistent_loop<MixedEngine<MID, FOORT_INTEGRATOR_RK4, D64>, true>(A, R);
+}
+
 const void* mixed_kernel_flat(int integrator, bool decide64) {
     if (integrator == FOORT_INTEGRATOR_RK4)
         return decide64 ? reinterpret_cast<const void*>(&integrate_mixed_kernel<kFlat, FOORT_INTEGRATOR_RK4, true>)
                         : reinterpret_cast<const void*>(&integrate_mixed_kernel<kFlat, FOORT_INTEGRATOR_RK4, false>);
     return decide64 ? reinterpret_cast<const void*>(&integrate_mixed_kernel<kFlat, FOORT_INTEGRATOR_VERLET, true>)
                     : reinterpret_cast<const void*>(&integrate_mixed_kernel<kFlat, FOORT_INTEGRATOR_VERLET, false>);
+}
+
+const void* mixed_pair_kernel_flat(bool decide64) {
+    static_assert(MixedEngine<kFlat, FOORT_INTEGRATOR_RK4, false>::kPairCapable, "pair kernel needs an inlined plugin");
+    return decide64 ? reinterpret_cast<const void*>(&integrate_mixed_pair_kernel<kFlat, true>)
+                    : reinterpret_cast<const void*>(&integrate_mixed_pair_kernel<kFlat, false>);
 }
 
 }  // namespace foort

@@ -206,10 +206,18 @@ __device__ __forceinline__ bool finite4(const double a[4]) {
 // warp publishes its step count, checks the step budget and the host cancel flag, and
 // learns whether another warp has asked every lane to stop. No loop waits on another
 // thread or on the host.
-template <class E>
+//
+// PAIR: lanes 2k and 2k+1 integrate one geodesic together (E::step_pair). Both take the
+// same pixel, hold the same state and so leave the loop together; the even lane writes
+// the record and counts the step.
+template <class E, bool PAIR = false>
 __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunConst& R) {
     const unsigned lane = threadIdx.x & 31u;
-    const unsigned lt_mask = (1u << lane) - 1u;
+    const bool odd = PAIR && (lane & 1u);
+    const unsigned slot_lane = PAIR ? (lane & ~1u) : lane;  // the lane that numbers the slot
+    const unsigned lt_mask = (1u << slot_lane) - 1u;
+    const unsigned slots = PAIR ? 0x55555555u : kFullMask;  // one bit per geodesic slot
+    const unsigned pmask = 3u << (lane & ~1u);
     typename E::Lane L;
     bool active = false;
     bool drained = false;
@@ -222,7 +230,7 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
     for (;;) {
         // Refill idle lanes from the queue.
         if (!drained) {
-            unsigned need = __ballot_sync(kFullMask, !active);
+            const unsigned need = __ballot_sync(kFullMask, !active) & slots;
             if (need) {
                 const int leader = __ffs(need) - 1;
                 const unsigned cnt = __popc(need);
@@ -235,9 +243,9 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                     if (my < A.n) {
                         const foort_pixel p = A.px[my];
                         if (stopping) {
-                            write_unstarted(&A.out[my], stop_err);
+                            if (!odd) write_unstarted(&A.out[my], stop_err);
                         } else if (p.image >= A.n_images || p.grid < 2) {
-                            write_unstarted(&A.out[my], FOORT_ERR_BADPIXEL);
+                            if (!odd) write_unstarted(&A.out[my], FOORT_ERR_BADPIXEL);
                         } else {
                             idx = my;
                             E::init(L, A.images[p.image], R, p);
@@ -255,11 +263,19 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
         for (;;) {
             if (active) {
                 const ImageConst& I = A.images[L.img];
-                ++lane_steps;
-                if (!E::step(L, I, R)) {
-                    E::finish(L, R, &A.out[idx]);
+                bool more;
+                if constexpr (PAIR) {
+                    more = E::step_pair(L, I, R, odd, pmask);
+                } else {
+                    more = E::step(L, I, R);
+                }
+                if (!odd) ++lane_steps;
+                if (!more) {
+                    if (!odd) {
+                        E::finish(L, R, &A.out[idx]);
+                        ++lane_done;
+                    }
                     active = false;
-                    ++lane_done;
                 }
             }
             ++since_poll;
@@ -294,7 +310,7 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                 stopping = true;
                 stop_err = (st & kStatusCancelled) ? FOORT_ERR_CANCELLED : FOORT_ERR_BUDGET;
                 if (active) {
-                    E::stop(L, R, &A.out[idx], stop_err);
+                    if (!odd) E::stop(L, R, &A.out[idx], stop_err);
                     active = false;
                 }
             }

@@ -175,6 +175,9 @@ __device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const Mixe
 
 template <int MID, int INTEG, bool DECIDE64>
 struct MixedEngine {
+    // step_pair exists for RK4 with an inlined plugin, without the FP64 near-horizon path
+    static constexpr bool kPairCapable = INTEG == FOORT_INTEGRATOR_RK4 && MixedMetric<MID>::kInline;
+
     struct Lane {
         ff x[4], v[4];
         ff lam;
@@ -367,18 +370,7 @@ struct MixedEngine {
                 rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])),
                     us, k4);
             }
-            // h / 6 is a quotient, not a product with a rounded 1/6: that constant is 3e-8
-            // too large, which would scale every velocity increment by the same factor
-            // and, amplified by strongly bent orbits, bias the escape direction by ~1e-7.
-            // One Newton-Raphson correction of h * (1/6) gives the quotient to within an
-            // ulp without that bias: q1 = q0 + (h - 6 q0) / 6.
-            const float q0 = __fmul_rn(h, 0.166666672f);
-            const float h6 = __fmaf_rn(__fmaf_rn(-6.f, q0, h), 0.166666672f, q0), hh6 = __fmul_rn(h, h6);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                du[i] = h6 * (k1[i] + 2.f * k2[i] + 2.f * k3[i] + k4[i]);
-                dxc[i] = hh6 * (k1[i] + k2[i] + k3[i]);
-            }
+            rk4_combine(h, k1, k2, k3, k4, du, dxc);
             L.rhs += 4;
         } else {
             // velocity Verlet (Integrators.cpp:99-152); the velocity change of each
@@ -431,10 +423,82 @@ struct MixedEngine {
                 }
             }
         }
-        // x += h u + dxc;  u += du;  lambda += h  (compensated). The increments are
-        // rounded to one float each (relative error 6e-8 of a step's change, unbiased,
-        // so it accumulates as a random walk); what the float-float sum prevents is the
-        // absorption of small increments into the large coordinate.
+        return advance(L, I, R, h, du, dxc);
+    }
+
+    // RK4's velocity increment du = h/6 (k1 + 2 k2 + 2 k3 + k4) and the O(h^2) part of the
+    // position increment dxc = h^2/6 (k1 + k2 + k3) (Integrators.cpp:91-92 rearranged).
+    static __device__ __forceinline__ void rk4_combine(float h, const float k1[4], const float k2[4],
+                                                       const float k3[4], const float k4[4], float du[4],
+                                                       float dxc[4]) {
+        // h / 6 is a quotient, not a product with a rounded 1/6: that constant is 3e-8
+        // too large, which would scale every velocity increment by the same factor
+        // and, amplified by strongly bent orbits, bias the escape direction by ~1e-7.
+        // One Newton-Raphson correction of h * (1/6) gives the quotient to within an
+        // ulp without that bias: q1 = q0 + (h - 6 q0) / 6.
+        const float q0 = __fmul_rn(h, 0.166666672f);
+        const float h6 = __fmaf_rn(__fmaf_rn(-6.f, q0, h), 0.166666672f, q0), hh6 = __fmul_rn(h, h6);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            du[i] = h6 * (k1[i] + 2.f * k2[i] + 2.f * k3[i] + k4[i]);
+            dxc[i] = hh6 * (k1[i] + k2[i] + k3[i]);
+        }
+    }
+
+    // One RK4 step of one geodesic on two lanes (Kerr and flat space, the inlined
+    // plugins). Both lanes hold the same state; in each of two rounds the even lane
+    // evaluates the metric part at stage 1 (then 3) and the odd lane at stage 2 (then 4),
+    // the positions that the reordered step of step() evaluates side by side. The four
+    // contractions run on both lanes, each kept by the lane whose metric it used, and
+    // each acceleration is sent to the partner with one shuffle. Both lanes then do the
+    // same arithmetic on the same values as step(), so they stay in lockstep and their
+    // results are step()'s. A lane does half the metric work of a step: where a launch
+    // has fewer geodesics than the GPU has lanes, a step's latency is what sets the pace.
+    static __device__ __forceinline__ bool step_pair(Lane& L, const ImageConst& I, const RunConst& R, bool odd,
+                                                     unsigned pmask) {
+        float uf[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) uf[i] = ff_f(L.v[i]);
+        const float h = adaptive_step_f32(R, I.mx, L.x[2], uf);
+        const float hh = 0.5f * h;
+        const bool rlog = R.rlog != 0;
+        float k1[4], k2[4], k3[4], k4[4], us[4], ka[4], du[4], dxc[4];
+        // stages 1 (even lane) and 2 (odd lane)
+        const ff p2r = ff_add_f(L.x[1], hh * uf[1]), p2t = ff_add_f(L.x[2], hh * uf[2]);
+        MetricAt<float> m = metric_part<MID, float>(I.mx.q, I.mx, rlog, odd ? p2r : L.x[1], odd ? p2t : L.x[2]);
+        accel_part(m, rlog, uf, ka);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) k1[i] = __shfl_sync(pmask, ka[i], 0, 2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
+        accel_part(m, rlog, us, ka);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) k2[i] = __shfl_sync(pmask, ka[i], 1, 2);
+        // stages 3 (even lane) and 4 (odd lane)
+        const ff p3r = ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])), p3t = ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2]));
+        const ff p4r = ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), p4t = ff_add_f(L.x[2], h * (uf[2] + hh * k2[2]));
+        m = metric_part<MID, float>(I.mx.q, I.mx, rlog, odd ? p4r : p3r, odd ? p4t : p3t);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
+        accel_part(m, rlog, us, ka);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) k3[i] = __shfl_sync(pmask, ka[i], 0, 2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
+        accel_part(m, rlog, us, ka);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) k4[i] = __shfl_sync(pmask, ka[i], 1, 2);
+        rk4_combine(h, k1, k2, k3, k4, du, dxc);
+        L.rhs += 2;  // the pair evaluates four
+        return advance(L, I, R, h, du, dxc);
+    }
+
+    // The end of a step: x += h u + dxc; u += du; lambda += h; terminations; diagnostics.
+    static __device__ __forceinline__ bool advance(Lane& L, const ImageConst& I, const RunConst& R, float h,
+                                                   const float du[4], const float dxc[4]) {
+        // The increments are rounded to one float each (relative error 6e-8 of a step's
+        // change, unbiased, so it accumulates as a random walk); what the float-float sum
+        // prevents is the absorption of small increments into the large coordinate.
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             L.x[i] = ff_add_f(L.x[i], __fmaf_rn(h, L.v[i].hi, dxc[i]));

@@ -23,6 +23,19 @@ const void* mixed_kernel_variant(int metric_id, int integ, bool decide64) {
 
 const void* mixed_kernel(int metric_id, int integ) { return mixed_kernel_variant(metric_id, integ, true); }
 
+const void* mixed_pair_kernel_kerr(bool decide64);
+const void* mixed_pair_kernel_flat(bool decide64);
+
+// Two-lane kernels: RK4 with the inlined plugins (Kerr, flat space).
+const void* mixed_pair_kernel_variant(int metric_id, int integ, bool decide64) {
+    if (integ != FOORT_INTEGRATOR_RK4) return nullptr;
+    switch (metric_id) {
+    case kKerr: return mixed_pair_kernel_kerr(decide64);
+    case kFlat: return mixed_pair_kernel_flat(decide64);
+    default: return nullptr;
+    }
+}
+
 void fill_mixed_constants(int metric_id, ImageConst& ic, const RunConst& rc) {
     MixedConst& mx = ic.mx;
     for (int i = 0; i < 6; ++i) mx.q[i] = static_cast<float>(ic.m.q[i]);

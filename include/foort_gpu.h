@@ -181,7 +181,7 @@ typedef struct foort_stats {
     uint32_t status;         /* FOORT_OK or the launch's FOORT_E_* code             */
     uint32_t n_blocks;
     uint32_t block_size;
-    uint32_t reserved;
+    uint32_t lanes_per_geodesic; /* 1, or 2 where two lanes integrated each geodesic   */
 } foort_stats;
 
 typedef struct foort_ctx foort_ctx;
@@ -254,6 +254,14 @@ int foort_gpu_cancel(foort_ctx* ctx);
 
 /* Launch shape override (0 = autotuned default). */
 int foort_gpu_set_launch(foort_ctx* ctx, uint32_t block_size, uint32_t blocks_per_sm);
+
+/* Lanes per geodesic in mixed precision with RK4 and the Kerr or flat metric: 0 chooses
+ * per launch (two lanes when the launch's geodesics, at two lanes each, fit on the GPU's
+ * resident lanes: a step's latency then sets the pace, and two lanes halve the metric
+ * work on it), 1 or 2 force the choice; other configurations always use one. Results
+ * are the same either way. No counterpart in the reference (one OpenMP thread per
+ * geodesic, Main.cpp:327-414). */
+int foort_gpu_set_lanes(foort_ctx* ctx, uint32_t lanes_per_geodesic);
 
 int foort_gpu_get_stats(const foort_ctx* ctx, foort_stats* stats);
 

@@ -107,6 +107,30 @@ def test_mixed_large_sample_vs_fp64(eng):
     assert s["median"] < MIXED_MEDIAN_TOL and s["p90"] < MIXED_P90_TOL
 
 
+@pytest.mark.parametrize("case", ["c2", "c1"])
+def test_two_lanes_per_geodesic_give_the_one_lane_results(eng, case):
+    """The two-lane kernel (foort_gpu_set_lanes) does step()'s arithmetic on the same
+    values, split over two lanes: every field of every record must be identical."""
+    wl = workloads.c2() if case == "c2" else workloads.c1()
+    wl.desc.precision = abi.PREC_MIXED
+    rng = np.random.default_rng(3)
+    side = 509 if case == "c2" else 100
+    idx = np.sort(rng.choice(side * side, 3000, replace=False))
+    px = np.zeros(len(idx), dtype=abi.PIXEL_DTYPE)
+    px["row"], px["col"], px["grid"] = idx // side, idx % side, side
+    out = {}
+    with eng.Engine(wl.desc) as e:
+        for lanes in (1, 2, 0):
+            e.set_lanes(lanes)
+            out[lanes] = e.integrate(px)
+            st = e.stats()
+            assert st["lanes_per_geodesic"] == (lanes or 2), st  # 3,000 geodesics: two lanes fit
+            assert st["geodesics"] == len(px)
+    for name in abi.RESULT_DTYPE.names:
+        np.testing.assert_array_equal(out[2][name], out[1][name], err_msg=name)
+        np.testing.assert_array_equal(out[0][name], out[1][name], err_msg=name)
+
+
 def test_mixed_budget_and_cancel_paths(eng):
     wl = workloads.c1(precision=abi.PREC_MIXED)
     px = abi.square_pixels(60)
