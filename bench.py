@@ -46,6 +46,9 @@ UNIT = "geodesics/s"
 OPS_PER_STEP = {("kerr", "rk4"): 1130, ("johannsen", "rk4"): 1650, ("johannsen", "verlet"): 830}
 SINCOS_PER_STEP = {("kerr", "rk4"): 20, ("johannsen", "rk4"): 20, ("johannsen", "verlet"): 10}
 OPS_PER_EXTRA_VERLET_RHS = 380
+# DRAM traffic per geodesic of the mixed kernel (dram__bytes_read.sum + dram__bytes_write.sum
+# of one ncu capture divided by its geodesics; profiles/integrate_mixed_pair_kernel_c2.md)
+DRAM_BYTES_PER_GEODESIC = {("kerr", "rk4"): 107.3}
 
 
 from foort_gb300.multirank import dist_env  # noqa: E402
@@ -250,11 +253,13 @@ def run_profile_case(args):
         px = np.zeros(len(idx), dtype=abi.PIXEL_DTYPE)
         px["row"], px["col"], px["grid"] = idx // side, idx % side, side
         with foort_gb300.Engine(wl.desc) as e:
+            e.set_lanes(args.lanes)
             e.integrate(px[:512])
             res = e.integrate(px)
             st = e.stats()
         out[name] = {"pixels": len(px), "kernel_ms": st["kernel_ms"], "steps": st["steps"],
                      "rhs_evals": st["rhs_evals"], "blocks": st["n_blocks"], "block_size": st["block_size"],
+                     "lanes_per_geodesic": st["lanes_per_geodesic"],
                      "geodesics": int(st["geodesics"]), "mean_steps": float(res["steps"].mean())}
     print(json.dumps({"profile_case": args.workload, **out}), flush=True)
     return 0
@@ -299,6 +304,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--profile-precision", default="both", choices=["both", "mixed", "fp64"])
+    ap.add_argument("--lanes", type=int, default=0, choices=[0, 1, 2],
+                    help="lanes per geodesic of the mixed kernel: 0 chosen per launch (default), 1 or 2")
     ap.add_argument("--profile", type=int, default=0, metavar="N",
                     help="profiling case: one launch of the mixed and one of the FP64 kernel on N pixels of "
                          "the workload's grid (after one warm-up launch each), then exit")
@@ -341,6 +348,7 @@ def main():
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
     rhs_per_round = [0] * len(rounds)
+    lanes_per_round = [1] * len(rounds)
 
     def device_step(e):
         kms = []
@@ -351,11 +359,13 @@ def main():
                 st = e.stats()
                 kms.append(st["kernel_ms"])
                 rhs_per_round[i] = st["rhs_evals"]
+                lanes_per_round[i] = st["lanes_per_geodesic"]
         return kms
 
     # ---- value: device-resident inputs
     peaks = foort_gb300.measure_peaks()
     with foort_gb300.Engine(wl.desc) as e:
+        e.set_lanes(args.lanes)
         for _ in range(args.warmup):
             device_step(e)
         barrier()
@@ -376,6 +386,7 @@ def main():
         barrier()
         clk = clocks.stop()
         mixed_res = [np.frombuffer(do.cpu().numpy().tobytes(), dtype=abi.RESULT_DTYPE) for do in d_out]
+        mixed_rhs, mixed_lanes = list(rhs_per_round), list(lanes_per_round)  # the FP64 leg reuses device_step
     t_step = max_over_ranks(sum(step_ms) / len(step_ms))
     value = world * n_geod / (t_step * 1e-3)
     steps_total = sum(int(r["steps"].sum()) for r in mixed_res)
@@ -409,6 +420,7 @@ def main():
         run_meshes(foort_gb300, e, wl, integrate)
 
     with foort_gb300.Engine(wl.desc) as e:
+        e.set_lanes(args.lanes)
         for _ in range(args.warmup):
             e2e_step(e)
         barrier()
@@ -449,27 +461,24 @@ def main():
     per_launch_ms = [launch_ms[i::n_launch] for i in range(n_launch)]
     big = int(np.argmax([len(r) for r in rounds]))
     big_ms = statistics.mean(per_launch_ms[big])
-    big_rhs = rhs_per_round[big]
+    big_rhs = mixed_rhs[big]
     big_steps = int(mixed_res[big]["steps"].sum())
     ops = OPS_PER_STEP.get(mkind, 1130)
     big_ops = big_steps * ops
     if mkind[1] == "verlet":  # every velocity iteration beyond the two base evaluations
         big_ops += OPS_PER_EXTRA_VERLET_RHS * max(0, big_rhs - 2 * big_steps)
     achieved = big_ops / (big_ms * 1e-3) / 1e12
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "traffic_per_geodesic.json")
-    if os.path.exists(prof):
-        try:
-            tpg = json.load(open(prof)).get(f"{mkind[0]}_{mkind[1]}_mixed")
-            if tpg:
-                traffic = tpg * len(rounds[big])
-        except (ValueError, OSError):
-            traffic = None
+    # DRAM bytes (read + write) of one launch, from ncu's per-geodesic figure scaled to the
+    # launch's geodesics (the capture is a 6,000-geodesic sample of the same grid)
+    tpg = DRAM_BYTES_PER_GEODESIC.get(mkind)
+    traffic = tpg * len(rounds[big]) if tpg else None
     roofline = {"bound": "alu-fp32", "achieved": achieved, "peak": peaks[0], "unit": "TFLOP/s",
-                "frac": achieved / peaks[0], "traffic": traffic,
+                "frac": achieved / peaks[0], "traffic": traffic, "traffic_unit": "bytes per launch",
                 "ops_per_step": ops, "sincos_per_step": SINCOS_PER_STEP.get(mkind, 20),
                 "peak_source": "FP32 FMA microbenchmark on this GPU (foort_measure_peaks); MEASURED_PEAKS.json "
-                               "has no FP32/FP64 entry", "kernel": "integrate_mixed_kernel",
+                               "has no FP32/FP64 entry",
+                "kernel": "integrate_mixed_pair_kernel" if mixed_lanes[big] == 2 else "integrate_mixed_kernel",
+                "lanes_per_geodesic": mixed_lanes[big],
                 "launch_ms": big_ms, "steps_per_launch": big_steps,
                 "fp64_peak_tflops": peaks[1]}
 
