@@ -71,6 +71,14 @@ def load():
     lib.foort_mesh_end_current_loop.argtypes = [vp]
     lib.foort_mesh_destroy.argtypes = [vp]
     lib.foort_mesh_destroy.restype = None
+    lib.foort_mesh_description.argtypes = [vp, C.c_char_p, u64]
+    lib.foort_first_line_info.argtypes = [C.POINTER(abi.RunDesc), u32, vp, C.c_char_p, u64]
+    lib.foort_output_create.argtypes = [C.POINTER(abi.OutputDesc), C.POINTER(vp)]
+    lib.foort_output_round.argtypes = [vp, vp, vp, u64]
+    lib.foort_output_finish.argtypes = [vp]
+    lib.foort_output_destroy.argtypes = [vp]
+    lib.foort_output_destroy.restype = None
+    lib.foort_gpu_run.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), u32, C.POINTER(u64), C.POINTER(u32)]
     _LIB = lib
     return lib
 
@@ -151,6 +159,16 @@ class Engine:
     def set_lanes(self, lanes_per_geodesic=0):
         """0: chosen per launch; 1 or 2 lanes per geodesic where the kernel has both."""
         self._check(self._lib.foort_gpu_set_lanes(self._ctx, lanes_per_geodesic))
+
+    def run(self, meshes, outputs=None):
+        """A whole run over one mesh (and optional Output) per image (foort_gpu_run).
+        Returns (geodesics, rounds)."""
+        n = len(meshes)
+        ms = (C.c_void_p * n)(*[m._m for m in meshes])
+        os_ = (C.c_void_p * n)(*[(o._o if o is not None else None) for o in (outputs or [None] * n)])
+        g, r = C.c_uint64(), C.c_uint32()
+        self._check(self._lib.foort_gpu_run(self._ctx, ms, os_, n, C.byref(g), C.byref(r)))
+        return g.value, r.value
 
     def stats(self):
         s = abi.Stats()
@@ -240,10 +258,70 @@ class Mesh:
     def end_round(self):
         self._lib.foort_mesh_end_current_loop(self._m)
 
+    def description(self):
+        buf = C.create_string_buffer(1024)
+        if self._lib.foort_mesh_description(self._m, buf, len(buf)) != 0:
+            raise FoortError(abi.FOORT_E_BADARG, "mesh description failed")
+        return buf.value.decode()
+
+    def first_line_info(self, desc, image=0):
+        """Utilities::GetFirstLineInfoString for image `image` of desc run on this mesh."""
+        buf = C.create_string_buffer(8192)
+        rc = self._lib.foort_first_line_info(C.byref(desc), image, self._m, buf, len(buf))
+        if rc != 0:
+            raise FoortError(rc, "first-line description failed")
+        return buf.value.decode()
+
     def close(self):
         if self._m:
             self._lib.foort_mesh_destroy(self._m)
             self._m = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Output:
+    """Output files of a run as FOORT writes them (include/foort_gpu.h foort_output_*)."""
+
+    def __init__(self, prefix, diag_flags, value_diag, first_line="", extension="dat", timestamp="",
+                 outputs_to_cache=1 << 40, geodesics_per_file=1 << 40):
+        self._lib = load()
+        self._o = C.c_void_p()
+        d = abi.OutputDesc()
+        d.prefix, d.timestamp, d.extension = prefix.encode(), timestamp.encode(), extension.encode()
+        d.first_line = first_line.encode()
+        d.outputs_to_cache, d.geodesics_per_file = outputs_to_cache, geodesics_per_file
+        d.diag_flags, d.value_diag = diag_flags, value_diag
+        rc = self._lib.foort_output_create(C.byref(d), C.byref(self._o))
+        if rc != 0:
+            raise FoortError(rc, "output creation failed")
+
+    def round(self, px, res):
+        px = np.ascontiguousarray(px, dtype=abi.PIXEL_DTYPE)
+        res = np.ascontiguousarray(res, dtype=abi.RESULT_DTYPE)
+        rc = self._lib.foort_output_round(self._o, px.ctypes.data, res.ctypes.data, len(px))
+        if rc != 0:
+            raise FoortError(rc, "writing output failed")
+
+    def finish(self):
+        rc = self._lib.foort_output_finish(self._o)
+        if rc != 0:
+            raise FoortError(rc, "writing output failed")
+
+    def close(self):
+        if self._o:
+            self._lib.foort_output_destroy(self._o)
+            self._o = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
     def __del__(self):
         try:

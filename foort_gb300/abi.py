@@ -15,6 +15,7 @@ FOORT_E_BUDGET = -3
 FOORT_E_NUMERIC = -4
 FOORT_E_CANCELLED = -5
 FOORT_E_UNSUPPORTED = -6
+FOORT_E_IO = -7
 
 # Metrics (Metric.h:78-189)
 METRIC_KERR = 0
@@ -146,6 +147,19 @@ class Stats(C.Structure):
         ("n_blocks", C.c_uint32),
         ("block_size", C.c_uint32),
         ("lanes_per_geodesic", C.c_uint32),
+    ]
+
+
+class OutputDesc(C.Structure):
+    _fields_ = [
+        ("prefix", C.c_char_p),
+        ("timestamp", C.c_char_p),
+        ("extension", C.c_char_p),
+        ("first_line", C.c_char_p),
+        ("outputs_to_cache", C.c_uint64),
+        ("geodesics_per_file", C.c_uint64),
+        ("diag_flags", C.c_uint32),
+        ("value_diag", C.c_uint32),
     ]
 
 

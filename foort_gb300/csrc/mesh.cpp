@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/foort_gpu.h"
+#include "diag_order.h"
 
 namespace {
 
@@ -24,14 +25,7 @@ namespace {
 // That vector is built in the order FourColor, GeodesicPosition, EquatorialPasses,
 // ClosestRadius, and appending the value diagnostic rotates it left by one.
 uint32_t first_diagnostic(uint32_t diag_flags, uint32_t value_diag) {
-    std::vector<uint32_t> order;
-    const uint32_t all[4] = {FOORT_DIAG_FOUR_COLOR_SCREEN, FOORT_DIAG_GEODESIC_POSITION, FOORT_DIAG_EQUATORIAL_PASSES,
-                             FOORT_DIAG_CLOSEST_RADIUS};
-    for (uint32_t f : all) {
-        if (!(diag_flags & f)) continue;
-        order.push_back(f);
-        if (value_diag & f) std::rotate(order.begin(), order.begin() + 1, order.end());
-    }
+    const std::vector<uint32_t> order = foort::diagnostic_order(diag_flags, value_diag);
     return order.empty() ? 0u : order[0];
 }
 
@@ -69,6 +63,7 @@ struct foort_mesh {
     virtual void end_loop() = 0;
     virtual bool done() const = 0;
     virtual uint64_t rounds() const = 0;
+    virtual std::string description() const = 0;  // Mesh::getFullDescriptionStr
 };
 
 namespace {
@@ -86,6 +81,10 @@ struct SimpleMesh final : foort_mesh {
     void end_loop() override { fin = true; }
     bool done() const override { return fin; }
     uint64_t rounds() const override { return fin ? 1 : 0; }
+    // Mesh.cpp:69-73
+    std::string description() const override {
+        return "Mesh: simple square grid (" + std::to_string(grid) + "^2 pixels)";
+    }
 };
 
 // SquareSubdivisionMeshV2, Mesh.cpp:660-1186
@@ -224,6 +223,16 @@ struct V2Mesh final : foort_mesh {
     void finished(uint64_t i, std::vector<double> v) override { queue[i]->value = std::move(v); }
     bool done() const override { return queue.empty(); }
     uint64_t rounds() const override { return n_rounds; }
+    // Mesh.cpp:697-707
+    std::string description() const override {
+        const uint64_t n = static_cast<uint64_t>(std::sqrt(static_cast<double>(initial)));
+        return "Mesh: square subdivision v2 (initial pixels: " + std::to_string(n) +
+               "^2; max subdivision: " + std::to_string(max_sub) +
+               "; pixels subdivided per iteration: " + std::to_string(iteration) +
+               "; max total pixels: " + (infinite ? std::string("infinite") : std::to_string(max_pixels)) +
+               "; if pixel is initially subdivided, will continue to max: " + std::to_string(sub_to_final ? 1 : 0) +
+               "; row/column size: " + std::to_string(grid) + ")";
+    }
 
     // EndCurrentLoop, Mesh.cpp:1092-1186
     void end_loop() override {
@@ -336,5 +345,13 @@ int foort_mesh_end_current_loop(foort_mesh* m) {
 }
 
 void foort_mesh_destroy(foort_mesh* m) { delete m; }
+
+int foort_mesh_description(const foort_mesh* m, char* buf, uint64_t cap) {
+    if (!m || !buf || cap == 0) return FOORT_E_BADARG;
+    const std::string s = m->description();
+    if (s.size() + 1 > cap) return FOORT_E_BADARG;
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+    return FOORT_OK;
+}
 
 }  // extern "C"

@@ -1,0 +1,65 @@
+// A whole run: the round loop of Main.cpp:313-419 over the engine, the meshes and the
+// output files, all through the C ABI.
+//
+// Per round every unfinished image's mesh hands out its pixels (ViewScreen::
+// getCurNrGeodesics / SetNewInitialConditions); the pixels of all images go to the GPU
+// in one launch (foort_gpu_integrate); the results go back to each mesh
+// (GeodesicFinished, Main.cpp:399) and to each image's output files
+// (NewGeodesicOutput, Main.cpp:400); then each mesh ends its round (EndCurrentLoop,
+// Main.cpp:410). Images advance in lockstep, so a round is one launch over all images.
+#include <cstring>
+#include <vector>
+
+#include "../../include/foort_gpu.h"
+
+extern "C" int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs,
+                             uint32_t n_images, uint64_t* geodesics, uint32_t* rounds) {
+    if (!ctx || !meshes || n_images == 0) return FOORT_E_BADARG;
+    for (uint32_t i = 0; i < n_images; ++i)
+        if (!meshes[i]) return FOORT_E_BADARG;
+    uint64_t total = 0;
+    uint32_t n_rounds = 0;
+    std::vector<foort_pixel> px;
+    std::vector<foort_result> res;
+    std::vector<uint64_t> count(n_images);
+    int rc = FOORT_OK;
+    for (;;) {
+        uint64_t n = 0;
+        for (uint32_t i = 0; i < n_images; ++i) {
+            const int fin = foort_mesh_is_finished(meshes[i]);
+            if (fin < 0) return fin;
+            count[i] = fin ? 0 : foort_mesh_cur_nr_geodesics(meshes[i]);
+            n += count[i];
+        }
+        bool any = false;
+        for (uint32_t i = 0; i < n_images; ++i) any = any || foort_mesh_is_finished(meshes[i]) == 0;
+        if (!any) break;
+        px.resize(n);
+        res.resize(n);
+        uint64_t k = 0;
+        for (uint32_t i = 0; i < n_images; ++i) {
+            if (foort_mesh_is_finished(meshes[i])) continue;
+            if ((rc = foort_mesh_get_pixels(meshes[i], i, px.data() + k))) return rc;
+            k += count[i];
+        }
+        rc = foort_gpu_integrate(ctx, px.data(), n, res.data());
+        if (rc != FOORT_OK) return rc;
+        k = 0;
+        for (uint32_t i = 0; i < n_images; ++i) {
+            if (foort_mesh_is_finished(meshes[i])) continue;
+            if ((rc = foort_mesh_set_results(meshes[i], res.data() + k, count[i]))) return rc;
+            if (outputs && outputs[i] && (rc = foort_output_round(outputs[i], px.data() + k, res.data() + k, count[i])))
+                return rc;
+            if ((rc = foort_mesh_end_current_loop(meshes[i]))) return rc;
+            k += count[i];
+        }
+        total += n;
+        ++n_rounds;
+    }
+    if (outputs)
+        for (uint32_t i = 0; i < n_images; ++i)
+            if (outputs[i] && (rc = foort_output_finish(outputs[i]))) return rc;
+    if (geodesics) *geodesics = total;
+    if (rounds) *rounds = n_rounds;
+    return FOORT_OK;
+}

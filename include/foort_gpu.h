@@ -37,6 +37,7 @@ extern "C" {
 #define FOORT_E_NUMERIC (-4)     /* at least one geodesic hit a non-finite state       */
 #define FOORT_E_CANCELLED (-5)   /* foort_gpu_cancel() stopped the launch             */
 #define FOORT_E_UNSUPPORTED (-6) /* option combination this build does not implement  */
+#define FOORT_E_IO (-7)          /* an output file could not be opened or written      */
 
 /* ---- plugin ids ------------------------------------------------------------------ */
 /* Metric classes of Metric.h:78-189; the names follow Config.cpp:153-290. */
@@ -335,6 +336,48 @@ int foort_mesh_set_results(foort_mesh* mesh, const foort_result* results, uint64
 int foort_mesh_end_current_loop(foort_mesh* mesh);
 
 void foort_mesh_destroy(foort_mesh* mesh);
+
+/* The mesh's Mesh::getFullDescriptionStr() (Mesh.cpp:69-73, 697-707) into buf. */
+int foort_mesh_description(const foort_mesh* mesh, char* buf, uint64_t cap);
+
+/* ---- Output files (GeodesicOutputHandler, InputOutput.h:40-110) -------------------------
+ * Writes a run's results as FOORT does, byte for byte: one file per diagnostic, named
+ * prefix_[timestamp_]Name[_n].ext, each starting with the first-line description, then
+ * "row col  value" per geodesic; outputs are cached up to outputs_to_cache geodesics and
+ * split over files of geodesics_per_file lines (InputOutput.cpp:95-330). */
+typedef struct foort_output_desc {
+    const char* prefix;          /* FilePrefix (may contain directories; created)         */
+    const char* timestamp;       /* "" or NULL for none                                   */
+    const char* extension;       /* e.g. "dat"; "" or NULL for none                       */
+    const char* first_line;      /* first line of every file; "" or NULL for none         */
+    uint64_t outputs_to_cache;   /* GeodesicOutputHandler's nroutputstocache              */
+    uint64_t geodesics_per_file; /* geodperfile (> 0; 0 is console output: unsupported)   */
+    uint32_t diag_flags;         /* the run's diagnostics and value diagnostic: they set  */
+    uint32_t value_diag;         /* the files' order (CreateDiagnosticVector)             */
+} foort_output_desc;
+
+typedef struct foort_output foort_output;
+
+/* Utilities::GetFirstLineInfoString (Utilities.cpp:52-84) for image `image` of the
+ * descriptor and its mesh, into buf (NUL-terminated). */
+int foort_first_line_info(const foort_run_desc* desc, uint32_t image, const foort_mesh* mesh, char* buf,
+                          uint64_t cap);
+int foort_output_create(const foort_output_desc* desc, foort_output** out);
+/* One round's results (host arrays, pixel order): PrepareForOutput(n) and n
+ * NewGeodesicOutput calls (Main.cpp:334, :400). FOORT_E_IO on a file error. */
+int foort_output_round(foort_output* out, const foort_pixel* px, const foort_result* res, uint64_t n);
+/* OutputFinished (InputOutput.cpp:123-127): write what is cached. */
+int foort_output_finish(foort_output* out);
+void foort_output_destroy(foort_output* out);
+
+/* A whole run: the round loop of Main.cpp:313-419. meshes[i] (and, unless NULL,
+ * outputs[i]) belong to image i of the context's descriptor. Each round integrates the
+ * pixels of every unfinished mesh in one launch (foort_gpu_integrate), passes the
+ * results to the meshes (Main.cpp:399) and output files (Main.cpp:400), and ends the
+ * meshes' rounds (Main.cpp:410); the outputs are finished at the end. Optional
+ * geodesics / rounds receive the totals. */
+int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs, uint32_t n_images,
+                  uint64_t* geodesics, uint32_t* rounds);
 
 #ifdef __cplusplus
 }
