@@ -79,6 +79,10 @@ def load():
     lib.foort_output_destroy.argtypes = [vp]
     lib.foort_output_destroy.restype = None
     lib.foort_gpu_run.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), u32, C.POINTER(u64), C.POINTER(u32)]
+    lib.foort_config_load.argtypes = [C.c_char_p, C.POINTER(abi.Config), C.c_char_p, u64]
+    lib.foort_config_parse.argtypes = [C.c_char_p, C.POINTER(abi.Config), C.c_char_p, u64]
+    lib.foort_config_create_mesh.argtypes = [C.POINTER(abi.Config), C.POINTER(vp)]
+    lib.foort_timestamp_string.argtypes = [C.c_char_p, u64]
     _LIB = lib
     return lib
 
@@ -87,8 +91,8 @@ def check_layout():
     """Compare the ctypes layouts with the compiled library's struct sizes."""
     lib = load()
     want = [C.sizeof(abi.Pixel), C.sizeof(abi.Result), C.sizeof(abi.RunDesc), C.sizeof(abi.ImageDesc),
-            C.sizeof(abi.Stats)]
-    got = [lib.foort_abi_size(i) for i in range(5)]
+            C.sizeof(abi.Stats), C.sizeof(abi.OutputDesc), C.sizeof(abi.Config)]
+    got = [lib.foort_abi_size(i) for i in range(len(want))]
     if want != got:
         raise FoortError(abi.FOORT_E_BADARG, f"ABI layout mismatch: python {want} vs library {got}")
     return got
@@ -328,3 +332,63 @@ class Output:
             self.close()
         except Exception:
             pass
+
+
+def load_config(path=None, text=None):
+    """A FOORT .cfg file (or its text) read as the reference reads it
+    (foort_config_load). Returns (config, notes): config.run has its image attached."""
+    lib = load()
+    cfg = abi.Config()
+    notes = C.create_string_buffer(1 << 16)
+    if text is not None:
+        rc = lib.foort_config_parse(text.encode(), C.byref(cfg), notes, len(notes))
+    else:
+        rc = lib.foort_config_load(os.fsencode(path), C.byref(cfg), notes, len(notes))
+    if rc != 0:
+        raise FoortError(rc, notes.value.decode())
+    cfg.run.images = C.pointer(cfg.image)
+    cfg.run.n_images = 1
+    return cfg, [ln for ln in notes.value.decode().splitlines() if ln]
+
+
+def config_mesh(cfg):
+    """The mesh a configuration asks for (a Mesh object)."""
+    m = Mesh.__new__(Mesh)
+    m._lib = load()
+    m._m = C.c_void_p()
+    rc = m._lib.foort_config_create_mesh(C.byref(cfg), C.byref(m._m))
+    if rc != 0:
+        raise FoortError(rc, "this mesh type is not available in the engine")
+    return m
+
+
+def run_config(path, precision=abi.PREC_MIXED, output_dir=None):
+    """A whole FOORT run from a .cfg file: the configured metric, diagnostics,
+    terminations, view screen, mesh, integrator and output files (Main.cpp:161-424), on
+    the GPU in the given precision. Relative output prefixes are taken from output_dir
+    (default: the working directory). Returns (geodesics, rounds, notes)."""
+    cfg, notes = load_config(path)
+    cfg.run.precision = precision
+    mesh = config_mesh(cfg)
+    out = None
+    prefix = cfg.file_prefix.decode()
+    if prefix:
+        if output_dir and not os.path.isabs(prefix):
+            prefix = os.path.join(output_dir, prefix)
+        ts = ""
+        if cfg.timestamp:
+            buf = C.create_string_buffer(32)
+            load().foort_timestamp_string(buf, len(buf))
+            ts = buf.value.decode()
+        first = mesh.first_line_info(cfg.run) if cfg.first_line_info else ""
+        out = Output(prefix, cfg.run.diag_flags, cfg.run.value_diag, first_line=first,
+                     extension=cfg.file_extension.decode(), timestamp=ts,
+                     outputs_to_cache=cfg.outputs_to_cache, geodesics_per_file=cfg.geodesics_per_file)
+    else:
+        notes.append("no output file prefix: results are not written (console output is not provided)")
+    with Engine(cfg.run) as e:
+        geodesics, rounds = e.run([mesh], [out])
+    if out is not None:
+        out.close()
+    mesh.close()
+    return geodesics, rounds, notes

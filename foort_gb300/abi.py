@@ -150,6 +150,34 @@ class Stats(C.Structure):
     ]
 
 
+CONFIG_MESH_SIMPLE = 0
+CONFIG_MESH_SUBDIVISION_V2 = 1
+CONFIG_MESH_SUBDIVISION = 2
+CONFIG_MESH_INPUT_PIXELS = 3
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("run", RunDesc),
+        ("image", ImageDesc),
+        ("mesh_kind", C.c_int32),
+        ("max_subdivide", C.c_int32),
+        ("total_pixels", C.c_uint64),
+        ("initial_pixels", C.c_uint64),
+        ("max_pixels", C.c_uint64),
+        ("iteration_pixels", C.c_uint64),
+        ("initial_sub_to_final", C.c_int32),
+        ("timestamp", C.c_int32),
+        ("outputs_to_cache", C.c_uint64),
+        ("geodesics_per_file", C.c_uint64),
+        ("first_line_info", C.c_int32),
+        ("screen_output_level", C.c_int32),
+        ("loop_message_frequency", C.c_uint64),
+        ("file_prefix", C.c_char * 1024),
+        ("file_extension", C.c_char * 64),
+    ]
+
+
 class OutputDesc(C.Structure):
     _fields_ = [
         ("prefix", C.c_char_p),

@@ -500,7 +500,7 @@ int foort_gpu_has_kernel(int32_t metric_id, int32_t integrator_id, int32_t preci
 }
 
 // Sizes of the ABI structs, for binding checks (0 pixel, 1 result, 2 run_desc,
-// 3 image_desc, 4 stats).
+// 3 image_desc, 4 stats, 5 output_desc, 6 config).
 uint64_t foort_abi_size(int32_t which) {
     switch (which) {
     case 0: return sizeof(foort_pixel);
@@ -508,6 +508,8 @@ uint64_t foort_abi_size(int32_t which) {
     case 2: return sizeof(foort_run_desc);
     case 3: return sizeof(foort_image_desc);
     case 4: return sizeof(foort_stats);
+    case 5: return sizeof(foort_output_desc);
+    case 6: return sizeof(foort_config);
     default: return 0;
     }
 }

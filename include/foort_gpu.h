@@ -291,7 +291,8 @@ int foort_metric_christoffel(int32_t metric_id, const double* metric_params, int
                              double* gamma);
 
 /* sizeof() of the ABI structs, for binding checks: 0 foort_pixel, 1 foort_result,
- * 2 foort_run_desc, 3 foort_image_desc, 4 foort_stats; 0 otherwise. Engine extension. */
+ * 2 foort_run_desc, 3 foort_image_desc, 4 foort_stats, 5 foort_output_desc,
+ * 6 foort_config; 0 otherwise. Engine extension. */
 uint64_t foort_abi_size(int32_t which);
 
 /* Measured FP32 and FP64 FMA throughput of the current GPU in TFLOP/s (an FMA counts as
@@ -369,6 +370,38 @@ int foort_output_round(foort_output* out, const foort_pixel* px, const foort_res
 /* OutputFinished (InputOutput.cpp:123-127): write what is cached. */
 int foort_output_finish(foort_output* out);
 void foort_output_destroy(foort_output* out);
+
+/* ---- FOORT configuration files (Main.cpp:161-200, Config.cpp:94-1155) --------------------
+ * Reads a .cfg file as the reference does (libconfig syntax, typed lookups without
+ * automatic conversion, the reference's defaults and fallbacks) into the descriptors of
+ * one run. `notes` receives the reference's default-setting messages, one per line. */
+#define FOORT_CONFIG_MESH_SIMPLE 0         /* SimpleSquareMesh                              */
+#define FOORT_CONFIG_MESH_SUBDIVISION_V2 1 /* SquareSubdivisionMeshV2                       */
+#define FOORT_CONFIG_MESH_SUBDIVISION 2    /* SquareSubdivisionMesh (V1): not in the engine */
+#define FOORT_CONFIG_MESH_INPUT_PIXELS 3   /* InputCertainPixelsMesh: not in the engine     */
+typedef struct foort_config {
+    foort_run_desc run;           /* n_images = 1; set run.images = &image before use   */
+    foort_image_desc image;       /* metric parameters, camera, screen                  */
+    int32_t mesh_kind;            /* FOORT_CONFIG_MESH_*                                 */
+    int32_t max_subdivide;
+    uint64_t total_pixels;        /* SimpleSquareMesh / InputCertainPixelsMesh          */
+    uint64_t initial_pixels, max_pixels, iteration_pixels;
+    int32_t initial_sub_to_final;
+    int32_t timestamp;            /* Output.TimeStamp: prefix_timestamp_ file names     */
+    uint64_t outputs_to_cache;    /* Output.GeodesicsToCache                            */
+    uint64_t geodesics_per_file;  /* Output.GeodesicsPerFile (0 read as unlimited)      */
+    int32_t first_line_info;      /* Output.FirstLineInfo                               */
+    int32_t screen_output_level;  /* Output.ScreenOutputLevel, 0..4                     */
+    uint64_t loop_message_frequency;
+    char file_prefix[1024];       /* Output.FilePrefix; "" = console output             */
+    char file_extension[64];
+} foort_config;
+int foort_config_load(const char* path, foort_config* cfg, char* notes, uint64_t cap);
+int foort_config_parse(const char* text, foort_config* cfg, char* notes, uint64_t cap);
+/* The configured mesh (FOORT_E_UNSUPPORTED for the V1 and input-pixels meshes). */
+int foort_config_create_mesh(const foort_config* cfg, foort_mesh** mesh);
+/* Utilities::GetTimeStampString (Utilities.cpp:28-36): local time, %y%m%d-%H%M%S. */
+int foort_timestamp_string(char* buf, uint64_t cap);
 
 /* A whole run: the round loop of Main.cpp:313-419. meshes[i] (and, unless NULL,
  * outputs[i]) belong to image i of the context's descriptor. Each round integrates the
