@@ -83,6 +83,10 @@ def load():
     lib.foort_config_parse.argtypes = [C.c_char_p, C.POINTER(abi.Config), C.c_char_p, u64]
     lib.foort_config_create_mesh.argtypes = [C.POINTER(abi.Config), C.POINTER(vp)]
     lib.foort_timestamp_string.argtypes = [C.c_char_p, u64]
+    lib.foort_gpu_positions.argtypes = [vp, vp, u64, vp, vp, vp, u64, C.POINTER(u64)]
+    lib.foort_geopos_count.argtypes = [C.POINTER(abi.RunDesc), u64, i32, C.POINTER(u64), C.POINTER(u64)]
+    lib.foort_output_round_positions.argtypes = [vp, vp, vp, u64, vp, vp]
+    lib.foort_gpu_get_desc.argtypes = [vp, C.POINTER(abi.RunDesc)]
     _LIB = lib
     return lib
 
@@ -163,6 +167,22 @@ class Engine:
     def set_lanes(self, lanes_per_geodesic=0):
         """0: chosen per launch; 1 or 2 lanes per geodesic where the kernel has both."""
         self._check(self._lib.foort_gpu_set_lanes(self._ctx, lanes_per_geodesic))
+
+    def positions(self, px, first):
+        """GeodesicPosition of the pixels whose first-pass results are `first`
+        (foort_gpu_positions). Returns (counts, points): points is (total, 4)."""
+        px = np.ascontiguousarray(px, dtype=abi.PIXEL_DTYPE)
+        first = np.ascontiguousarray(first, dtype=abi.RESULT_DTYPE)
+        n = len(px)
+        counts = np.zeros(n, dtype=np.uint64)
+        total = C.c_uint64()
+        self._check(self._lib.foort_gpu_positions(self._ctx, px.ctypes.data, n, first.ctypes.data,
+                                                  counts.ctypes.data, None, 0, C.byref(total)))
+        points = np.zeros((max(total.value, 1), 4))
+        self._check(self._lib.foort_gpu_positions(self._ctx, px.ctypes.data, n, first.ctypes.data,
+                                                  counts.ctypes.data, points.ctypes.data, total.value,
+                                                  C.byref(total)))
+        return counts, points[:total.value]
 
     def run(self, meshes, outputs=None):
         """A whole run over one mesh (and optional Output) per image (foort_gpu_run).
@@ -304,10 +324,19 @@ class Output:
         if rc != 0:
             raise FoortError(rc, "output creation failed")
 
-    def round(self, px, res):
+    def round(self, px, res, counts=None, points=None):
+        """One round's results; counts / points (Engine.positions) with GeodesicPosition."""
         px = np.ascontiguousarray(px, dtype=abi.PIXEL_DTYPE)
         res = np.ascontiguousarray(res, dtype=abi.RESULT_DTYPE)
-        rc = self._lib.foort_output_round(self._o, px.ctypes.data, res.ctypes.data, len(px))
+        if counts is None:
+            rc = self._lib.foort_output_round(self._o, px.ctypes.data, res.ctypes.data, len(px))
+        else:
+            counts = np.ascontiguousarray(counts, dtype=np.uint64)
+            points = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 4)
+            if len(points) == 0:
+                points = np.zeros((1, 4))
+            rc = self._lib.foort_output_round_positions(self._o, px.ctypes.data, res.ctypes.data, len(px),
+                                                        counts.ctypes.data, points.ctypes.data)
         if rc != 0:
             raise FoortError(rc, "writing output failed")
 

@@ -146,10 +146,6 @@ int validate(const foort_run_desc* d, std::string& why) {
     if (d->term_flags == 0) { why = "no terminations turned on"; return FOORT_E_BADARG; }
     if (d->term_flags & ~0xFu) { why = "unknown termination flag"; return FOORT_E_BADARG; }
     if (d->diag_flags & ~0xFu) { why = "unknown diagnostic flag"; return FOORT_E_BADARG; }
-    if (d->diag_flags & FOORT_DIAG_GEODESIC_POSITION) {
-        why = "GeodesicPosition needs per-step storage, which this entry point does not provide";
-        return FOORT_E_UNSUPPORTED;
-    }
     if (!(d->epsilon > 0.0) || !(d->derivative_h > 0.0)) { why = "epsilon and derivative_h must be > 0"; return FOORT_E_BADARG; }
     for (uint32_t i = 0; i < d->n_images; ++i) {
         const foort_image_desc& im = d->images[i];
@@ -192,6 +188,9 @@ RunConst make_run_const(const foort_run_desc& d) {
     R.poll_steps = 512;
     R.mixed_options = d.mixed_options;
     R.mixed_fp64_margin = (d.mixed_options & FOORT_MIXED_FP64_NEAR_HORIZON) ? d.mixed_fp64_margin : 0.0;
+    R.gp_every = d.geopos_freq.every_n;
+    R.gp_start = d.geopos_freq.at_start;
+    R.gp_finish = d.geopos_freq.at_finish;
     return R;
 }
 
@@ -265,7 +264,8 @@ int ensure_capacity(foort_ctx* ctx, uint64_t n) {
     return FOORT_OK;
 }
 
-int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, cudaStream_t st) {
+int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, cudaStream_t st,
+           const unsigned long long* gp_plan = nullptr, double* gp_out = nullptr) {
     LaunchShape ls;
     int rc = choose_launch(ctx, ctx->rc, n, ctx->num_sms, ctx->block_size, ctx->blocks_per_sm, ctx->lanes, ls);
     if (rc) return rc;
@@ -282,6 +282,8 @@ int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_
     A.ctr = ctx->d_ctr;
     A.cancel = ctx->d_cancel;
     A.budget = ctx->budget;
+    A.gp_plan = gp_plan;
+    A.gp_out = gp_out;
     if (!A.budget && !(ctx->rc.term_flags & FOORT_TERM_TIMEOUT)) {
         // Without TimeOut a geodesic may never terminate (the reference would loop
         // forever); a finite default budget keeps every launch finite.
@@ -300,6 +302,27 @@ int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_
     ctx->last_stream = st;
     ctx->pending = true;
     return FOORT_OK;
+}
+
+// GeodesicPosition samples of one geodesic (M) and the stride j of the kept ones, from its
+// step count. DecideUpdate (Diagnostics.cpp:113-140) runs at Geodesic::Reset and after
+// every step, so with UpdateFrequency N > 0 a geodesic of S steps has floor((S + 1) / N)
+// samples, with N = 0 one at the start and / or one at the finish. Geodesics that did not
+// terminate (stopped by the budget or a cancel, or skipped) have none. The end of
+// GeodesicPositionDiagnostic::UpdateData (:255-283) keeps every j-th sample, j =
+// M / OutputSteps, when OutputSteps is below M: (M - 1) / j + 1 of them.
+void geopos_plan(const foort_run_desc& d, uint64_t steps, int32_t term, uint64_t& M, uint64_t& j, uint64_t& kept) {
+    M = 0;
+    if (term != FOORT_TERMCODE_CONTINUE) {
+        const uint64_t every = d.geopos_freq.every_n;
+        if (every > 0)
+            M = (steps + 1) / every;
+        else
+            M = (d.geopos_freq.at_start ? 1u : 0u) + (d.geopos_freq.at_finish ? 1u : 0u);
+    }
+    const uint64_t K = d.geopos_output_steps;
+    j = (K > 0 && K < M) ? M / K : 1;
+    kept = M ? (M - 1) / j + 1 : 0;
 }
 
 int finish(foort_ctx* ctx) {
@@ -427,6 +450,69 @@ int foort_gpu_integrate_async(foort_ctx* ctx, const foort_pixel* d_px, uint64_t 
     return launch(ctx, d_px, n, d_out, static_cast<cudaStream_t>(cuda_stream));
 }
 
+int foort_gpu_positions(foort_ctx* ctx, const foort_pixel* px, uint64_t n, const foort_result* first, uint64_t* counts,
+                        double* points, uint64_t cap_points, uint64_t* total_points) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    if (n && (!px || !first || !counts)) return fail(ctx, FOORT_E_BADARG, "NULL pixel, result or count buffer");
+    if (!(ctx->desc.diag_flags & FOORT_DIAG_GEODESIC_POSITION))
+        return fail(ctx, FOORT_E_BADARG, "the GeodesicPosition diagnostic is not turned on");
+    std::vector<unsigned long long> plan(3 * n);
+    uint64_t total = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        uint64_t M, j, kept;
+        geopos_plan(ctx->desc, first[i].steps, first[i].term, M, j, kept);
+        plan[3 * i] = total;
+        plan[3 * i + 1] = j;
+        plan[3 * i + 2] = M;
+        counts[i] = kept;
+        total += kept;
+    }
+    if (total_points) *total_points = total;
+    if (!points || n == 0) return FOORT_OK;
+    if (cap_points < total)
+        return fail(ctx, FOORT_E_BADARG, "the points buffer holds " + std::to_string(cap_points) + " of the " +
+                                             std::to_string(total) + " positions");
+    int rc = finish(ctx);
+    if (rc != FOORT_OK && rc != FOORT_E_BUDGET && rc != FOORT_E_CANCELLED) return rc;
+    if ((rc = ensure_capacity(ctx, n))) return rc;
+    unsigned long long* d_plan = nullptr;
+    double* d_pts = nullptr;
+    std::vector<foort_result> again(n);
+    auto body = [&]() -> int {
+        cudaStream_t st = ctx->stream;
+        CK(cudaMalloc(&d_plan, plan.size() * sizeof(unsigned long long)));
+        CK(cudaMalloc(&d_pts, std::max<uint64_t>(1, total) * 4 * sizeof(double)));
+        CK(cudaMemsetAsync(d_pts, 0xFF, std::max<uint64_t>(1, total) * 4 * sizeof(double), st));  // NaN
+        CK(cudaMemcpyAsync(ctx->d_px, px, n * sizeof(foort_pixel), cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(d_plan, plan.data(), plan.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, st));
+        int r = launch(ctx, ctx->d_px, n, ctx->d_out, st, d_plan, d_pts);
+        if (r) return r;
+        CK(cudaMemcpyAsync(points, d_pts, total * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(again.data(), ctx->d_out, n * sizeof(foort_result), cudaMemcpyDeviceToHost, st));
+        return finish(ctx);
+    };
+    rc = body();
+    if (d_plan) cudaFree(d_plan);
+    if (d_pts) cudaFree(d_pts);
+    if (rc != FOORT_OK) return rc;
+    // the second pass must retrace the first: same steps for every recorded geodesic
+    for (uint64_t i = 0; i < n; ++i)
+        if (plan[3 * i + 2] && again[i].steps != first[i].steps)
+            return fail(ctx, FOORT_E_NUMERIC, "geodesic " + std::to_string(i) + " took " +
+                                                  std::to_string(again[i].steps) + " steps on the second pass, " +
+                                                  std::to_string(first[i].steps) + " on the first");
+    return FOORT_OK;
+}
+
+int foort_geopos_count(const foort_run_desc* desc, uint64_t steps, int32_t term, uint64_t* samples, uint64_t* kept) {
+    if (!desc) return FOORT_E_BADARG;
+    uint64_t M, j, k;
+    geopos_plan(*desc, steps, term, M, j, k);
+    if (samples) *samples = M;
+    if (kept) *kept = k;
+    return FOORT_OK;
+}
+
 int foort_gpu_sync(foort_ctx* ctx) {
     if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
     return finish(ctx);
@@ -457,6 +543,12 @@ int foort_gpu_set_lanes(foort_ctx* ctx, uint32_t lanes_per_geodesic) {
     if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
     if (lanes_per_geodesic > 2) return fail(ctx, FOORT_E_BADARG, "lanes_per_geodesic must be 0 (automatic), 1 or 2");
     ctx->lanes = lanes_per_geodesic;
+    return FOORT_OK;
+}
+
+int foort_gpu_get_desc(const foort_ctx* ctx, foort_run_desc* desc) {
+    if (!ctx || !desc) return FOORT_E_BADARG;
+    *desc = ctx->desc;  // images: the context's own copy
     return FOORT_OK;
 }
 

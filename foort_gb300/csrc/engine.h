@@ -72,6 +72,8 @@ struct RunConst {
     uint32_t mixed_options;
     uint32_t pad0;
     double mixed_fp64_margin;
+    uint64_t gp_every;  // GeodesicPosition update frequency (recorded on a second pass)
+    int32_t gp_start, gp_finish;
 };
 
 // Scratch counters of one launch (device memory, zeroed before each launch).
@@ -100,6 +102,10 @@ struct LaunchArgs {
     unsigned long long* ctr;          // kNumCtr counters
     const volatile int32_t* cancel;   // host flag in mapped pinned memory (may be null)
     unsigned long long budget;        // 0 = unlimited
+    // GeodesicPosition second pass (null otherwise): per pixel {first slot, stride j,
+    // samples M}, and the slots, 4 doubles each
+    const unsigned long long* gp_plan;
+    double* gp_out;
 };
 
 }  // namespace foort

@@ -86,6 +86,37 @@ __device__ __forceinline__ bool diag_decide(uint64_t every, int32_t at_start, in
     return false;
 }
 
+// GeodesicPosition (Diagnostics.cpp:246-284), recorded on a second, identical pass.
+// The reference saves every sampled position and at the end keeps the samples i with
+// i % j == 0, j = M / OutputSteps (M samples in all), the last kept one replaced by the
+// final sample. The first pass gives M (from the step count), so this pass writes each
+// kept sample straight to its slot: sample i goes to slot i / j, sample M - 1 to slot
+// (M - 1) / j. Samples beyond the M the plan allows are not written.
+struct GeoposRec {
+    double* dst;  // this geodesic's first slot; null: not recording
+    uint64_t j, M, i, cnt;
+};
+
+__device__ __forceinline__ void geopos_sample(GeoposRec& g, const RunConst& R, const double x[4], double lam,
+                                              int term) {
+    if (!diag_decide(R.gp_every, R.gp_start, R.gp_finish, g.cnt, lam, term)) return;
+    const uint64_t i = g.i++;
+    if (i >= g.M) return;
+    uint64_t slot;
+    if (i % g.j == 0) {
+        slot = i / g.j;
+    } else if (i == g.M - 1) {
+        slot = (g.M - 1) / g.j;
+    } else {
+        return;
+    }
+    double* d = g.dst + 4 * slot;
+    d[0] = x[0];
+    d[1] = x[1];
+    d[2] = x[2];
+    d[3] = x[3];
+}
+
 // FourColorScreenDiagnostic::UpdateData, Diagnostics.cpp:159-200 (only on BoundarySphere)
 static __device__ __noinline__ int32_t four_color_quadrant(double th, double ph) {
     if (fabs(ph) < 2 * kRefPi * 1e5) {
@@ -248,6 +279,16 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                             if (!odd) write_unstarted(&A.out[my], FOORT_ERR_BADPIXEL);
                         } else {
                             idx = my;
+                            L.gp.dst = nullptr;
+                            L.gp.j = 1;
+                            L.gp.M = 0;
+                            if (A.gp_plan && !odd && A.gp_plan[3 * my + 2] > 0 && A.gp_plan[3 * my + 1] > 0) {
+                                L.gp.dst = A.gp_out + 4 * A.gp_plan[3 * my];
+                                L.gp.j = A.gp_plan[3 * my + 1];
+                                L.gp.M = A.gp_plan[3 * my + 2];
+                            }
+                            L.gp.i = 0;
+                            L.gp.cnt = 0;
                             E::init(L, A.images[p.image], R, p);
                             active = true;
                         }

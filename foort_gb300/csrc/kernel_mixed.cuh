@@ -194,7 +194,16 @@ struct MixedEngine {
         uint32_t rhs = 0;
         uint32_t fp64 = 0;
         int32_t term = 0;
+        GeoposRec gp;  // set by the loop before init
     };
+
+    // GeodesicPosition sample of the compensated position (second pass only)
+    static __device__ __forceinline__ void geopos(Lane& L, const RunConst& R, double lam) {
+        double x[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) x[i] = ff_d(L.x[i]);
+        geopos_sample(L.gp, R, x, lam, L.term);
+    }
 
     static __device__ __forceinline__ void load_double(const Lane& L, double x[4], double v[4]) {
         for (int i = 0; i < 4; ++i) {
@@ -225,6 +234,7 @@ struct MixedEngine {
         L.T.cH = L.T.cB = L.T.cT = L.T.cTh = 0;
         L.T.tcur = 0;
         diags(L, I, R, true);  // Geodesic::Reset's start sample at lambda = 0
+        if (L.gp.dst) geopos(L, R, 0.0);
     }
 
     // EquatorialPasses and ClosestRadius updates (Diagnostics.cpp:351-380, :427-446) on
@@ -508,6 +518,7 @@ struct MixedEngine {
         ++L.steps;
         L.term = terms(L, I, R);
         diags(L, I, R, false);
+        if (L.gp.dst) geopos(L, R, 1.0);  // lambda > 0 after a step; only compared with 0
         // A NaN or Inf anywhere in the state reaches r or u^r within one step through the
         // right-hand side, so those two words stand for the whole state here; the full
         // state is checked again when the geodesic's record is written.

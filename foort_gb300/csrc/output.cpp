@@ -187,25 +187,52 @@ struct foort_output {
         return FOORT_OK;
     }
 
-    // The lines of geodesics [a, b) of a round for diagnostic k.
-    static void format(uint32_t diag, const foort_pixel* px, const foort_result* res, uint64_t a, uint64_t b,
-                       std::string& out, std::vector<uint64_t>& st, uint64_t base) {
+    // The lines of geodesics [a, b) of a round for diagnostic k. GeodesicPosition's string
+    // is the number of positions, " ;; ", then every coordinate with a space after it
+    // (Diagnostics.cpp:286-302).
+    static void format(uint32_t diag, const foort_pixel* px, const foort_result* res, const uint64_t* counts,
+                       const uint64_t* first, const double* points, uint64_t a, uint64_t b, std::string& out,
+                       std::vector<uint64_t>& st, uint64_t base) {
         char line[512];
         for (uint64_t i = a; i < b; ++i) {
             int n;
             const unsigned long long row = px[i].row, col = px[i].col;
+            st.push_back(base + out.size());
             switch (diag) {
             case FOORT_DIAG_FOUR_COLOR_SCREEN: n = std::snprintf(line, sizeof(line), "%llu %llu  %d\n", row, col, res[i].quadrant); break;
             case FOORT_DIAG_EQUATORIAL_PASSES: n = std::snprintf(line, sizeof(line), "%llu %llu  %d\n", row, col, res[i].equat_passes); break;
+            case FOORT_DIAG_GEODESIC_POSITION: {
+                n = std::snprintf(line, sizeof(line), "%llu %llu  %llu ;; ", row, col,
+                                  static_cast<unsigned long long>(counts[i]));
+                out.append(line, static_cast<size_t>(n));
+                const double* p = points + 4 * first[i];
+                for (uint64_t k = 0; k < 4 * counts[i]; ++k) {
+                    n = std::snprintf(line, sizeof(line), "%f ", p[k]);
+                    out.append(line, static_cast<size_t>(n));
+                }
+                out += '\n';
+                continue;
+            }
             default: n = std::snprintf(line, sizeof(line), "%llu %llu  %f\n", row, col, res[i].closest_r); break;
             }
-            st.push_back(base + out.size());
             out.append(line, static_cast<size_t>(n));
         }
     }
 
     // PrepareForOutput + NewGeodesicOutput for a whole round (InputOutput.cpp:95-121)
-    int round(const foort_pixel* px, const foort_result* res, uint64_t n) {
+    int round(const foort_pixel* px, const foort_result* res, uint64_t n, const uint64_t* counts = nullptr,
+              const double* points = nullptr) {
+        const bool geopos = std::find(diags.begin(), diags.end(), FOORT_DIAG_GEODESIC_POSITION) != diags.end();
+        if (geopos && n && (!counts || !points)) return FOORT_E_BADARG;
+        std::vector<uint64_t> first;
+        if (geopos) {
+            first.resize(n);
+            uint64_t s = 0;
+            for (uint64_t i = 0; i < n; ++i) {
+                first[i] = s;
+                s += counts[i];
+            }
+        }
         if (cached + n > cache_max) {
             const int rc = flush();
             if (rc) return rc;
@@ -216,7 +243,7 @@ struct foort_output {
         const uint64_t nchunks = (n + chunk - 1) / chunk;
         for (size_t k = 0; k < diags.size(); ++k) {
             if (nchunks <= 1 || hw == 1) {
-                format(diags[k], px, res, 0, n, text[k], starts[k], 0);
+                format(diags[k], px, res, counts, first.data(), points, 0, n, text[k], starts[k], 0);
                 continue;
             }
             std::vector<std::string> parts(nchunks);
@@ -226,7 +253,8 @@ struct foort_output {
             for (uint64_t t = 0; t < nt; ++t)
                 pool.emplace_back([&, t]() {
                     for (uint64_t c = t; c < nchunks; c += nt)
-                        format(diags[k], px, res, c * chunk, std::min(n, (c + 1) * chunk), parts[c], pst[c], 0);
+                        format(diags[k], px, res, counts, first.data(), points, c * chunk, std::min(n, (c + 1) * chunk), parts[c],
+                               pst[c], 0);
                 });
             for (auto& th : pool) th.join();
             for (uint64_t c = 0; c < nchunks; ++c) {
@@ -258,7 +286,6 @@ int foort_output_create(const foort_output_desc* od, foort_output** out) {
     // An empty prefix or zero geodesics per file means console output in the reference
     // (InputOutput.cpp:80-82); this writer only writes files.
     if (od->prefix[0] == '\0' || od->geodesics_per_file == 0) return FOORT_E_UNSUPPORTED;
-    if (od->diag_flags & FOORT_DIAG_GEODESIC_POSITION) return FOORT_E_UNSUPPORTED;
     const std::vector<uint32_t> order = foort::diagnostic_order(od->diag_flags, od->value_diag);
     if (order.empty()) return FOORT_E_BADARG;
     auto* o = new foort_output();
@@ -278,6 +305,12 @@ int foort_output_create(const foort_output_desc* od, foort_output** out) {
 int foort_output_round(foort_output* o, const foort_pixel* px, const foort_result* res, uint64_t n) {
     if (!o || (n && (!px || !res))) return FOORT_E_BADARG;
     return o->round(px, res, n);
+}
+
+int foort_output_round_positions(foort_output* o, const foort_pixel* px, const foort_result* res, uint64_t n,
+                                 const uint64_t* counts, const double* points) {
+    if (!o || (n && (!px || !res))) return FOORT_E_BADARG;
+    return o->round(px, res, n, counts, points);
 }
 
 int foort_output_finish(foort_output* o) {

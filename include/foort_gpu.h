@@ -240,6 +240,21 @@ int foort_gpu_integrate_async(foort_ctx* ctx, const foort_pixel* d_px, uint64_t 
 int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foort_pixel* d_px, uint64_t n,
                                 foort_result* d_out, void* cuda_stream, foort_stats* stats);
 
+/* GeodesicPosition (Diagnostics.cpp:246-284): the saved positions of each geodesic, after
+ * the reference's decimation to OutputSteps. `first` holds the results of the pixels'
+ * foort_gpu_integrate call (pass 1, same context); this call integrates them once more
+ * and records the kept positions. counts[i] receives the number of positions of
+ * geodesic i; points (host, 4 doubles per position: t, x1, theta, phi, with x1 = ln r in
+ * log-r mode as the reference stores it) receives them geodesic after geodesic. With
+ * points == NULL only counts and *total_points are filled (to size the buffer).
+ * FOORT_E_NUMERIC if the second pass did not retrace the first. */
+int foort_gpu_positions(foort_ctx* ctx, const foort_pixel* px, uint64_t n, const foort_result* first, uint64_t* counts,
+                        double* points, uint64_t cap_points, uint64_t* total_points);
+
+/* Number of GeodesicPosition samples of a geodesic of `steps` steps that ended with
+ * termination `term`, and how many of them the reference keeps. */
+int foort_geopos_count(const foort_run_desc* desc, uint64_t steps, int32_t term, uint64_t* samples, uint64_t* kept);
+
 /* Wait for the last async launch of this context and return its status. */
 int foort_gpu_sync(foort_ctx* ctx);
 
@@ -265,6 +280,9 @@ int foort_gpu_set_launch(foort_ctx* ctx, uint32_t block_size, uint32_t blocks_pe
 int foort_gpu_set_lanes(foort_ctx* ctx, uint32_t lanes_per_geodesic);
 
 int foort_gpu_get_stats(const foort_ctx* ctx, foort_stats* stats);
+
+/* The context's run descriptor (its images point to the context's own copy). */
+int foort_gpu_get_desc(const foort_ctx* ctx, foort_run_desc* desc);
 
 void foort_gpu_destroy(foort_ctx* ctx);
 
@@ -367,6 +385,10 @@ int foort_output_create(const foort_output_desc* desc, foort_output** out);
 /* One round's results (host arrays, pixel order): PrepareForOutput(n) and n
  * NewGeodesicOutput calls (Main.cpp:334, :400). FOORT_E_IO on a file error. */
 int foort_output_round(foort_output* out, const foort_pixel* px, const foort_result* res, uint64_t n);
+/* The same with the GeodesicPosition diagnostic: counts / points as foort_gpu_positions
+ * returns them (its line: "row col  count ;; t x1 theta phi ...", Diagnostics.cpp:286-302). */
+int foort_output_round_positions(foort_output* out, const foort_pixel* px, const foort_result* res, uint64_t n,
+                                 const uint64_t* counts, const double* points);
 /* OutputFinished (InputOutput.cpp:123-127): write what is cached. */
 int foort_output_finish(foort_output* out);
 void foort_output_destroy(foort_output* out);

@@ -143,8 +143,45 @@ def dat_runs():
         print("dat run", name, n.value, "geodesics", nr.value, "rounds")
 
 
+def geopos_workload(every, output_steps, value_geopos):
+    """Kerr a = 0.99 at 60 deg (the C2 view) with the GeodesicPosition diagnostic."""
+    wl = workloads.c2(abi.PREC_FP64)
+    d = wl.desc
+    d.diag_flags = abi.DIAG_GEODESIC_POSITION | (abi.DIAG_EQUATORIAL_PASSES if value_geopos else abi.DIAG_FOUR_COLOR_SCREEN)
+    d.value_diag = abi.DIAG_GEODESIC_POSITION if value_geopos else abi.DIAG_FOUR_COLOR_SCREEN
+    d.geopos_freq = abi.UpdateFreq(every, 0, 1)
+    d.geopos_output_steps = output_steps
+    return wl
+
+
+GEOPOS_RUNS = {
+    # name: (UpdateFrequency, OutputSteps, GeodesicPosition drives the mesh, mesh)
+    "geopos12": (1, 40, False, oracle.RefMeshSpec(0, 1, 12 * 12, 0, 0, 0, 0, 0)),
+    "geopos12f3": (3, 25, True, oracle.RefMeshSpec(0, 1, 12 * 12, 0, 0, 0, 0, 0)),
+    "geoposv2": (1, 8, True, oracle.RefMeshSpec(1, 2, 0, 0, 9 * 9, 30, 0, 0)),
+}
+
+
+def geopos_runs():
+    """Complete runs with GeodesicPosition, written by the reference built with strict
+    IEEE flags (so that the strict oracle retraces them step for step)."""
+    lib = oracle.ref_lib(strict=True)
+    for name, (every, steps, val, spec) in GEOPOS_RUNS.items():
+        wl = geopos_workload(every, steps, val)
+        prefix = os.path.join(HERE, "dat", name).encode()
+        n = C.c_uint64()
+        nr = C.c_uint32()
+        sec = C.c_double()
+        rc = lib.ref_run(C.byref(wl.desc), C.byref(spec), prefix, b"", b"dat", 1 << 40, 1 << 40, 1, 0, C.byref(n),
+                         C.byref(nr), C.byref(sec))
+        assert rc == 0
+        print("geopos run", name, n.value, "geodesics", nr.value, "rounds")
+
+
 def main(parts):
     oracle.build(with_ref=True)
+    if "geopos" in parts:
+        geopos_runs()
     if "mesh" in parts:
         mesh_traces()
         first_lines()

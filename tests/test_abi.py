@@ -69,8 +69,13 @@ def test_create_rejects_bad_descriptors_without_touching_the_gpu(engine_lib):
         foort_gb300.Engine(d)
     assert e.value.code == abi.FOORT_E_BADARG
     d.metric_id = abi.METRIC_KERR
-    d.diag_flags |= abi.DIAG_GEODESIC_POSITION
+    d.diag_flags |= 0x100  # no such diagnostic
     with pytest.raises(foort_gb300.FoortError) as e:
         foort_gb300.Engine(d)
-    assert e.value.code == abi.FOORT_E_UNSUPPORTED
+    assert e.value.code == abi.FOORT_E_BADARG
+    d.diag_flags = abi.DIAG_FOUR_COLOR_SCREEN
+    d.term_flags = 0  # no termination
+    with pytest.raises(foort_gb300.FoortError) as e:
+        foort_gb300.Engine(d)
+    assert e.value.code == abi.FOORT_E_BADARG
     del keep

@@ -6,10 +6,13 @@ tests/golden/dat: a 40^2 SimpleSquareMesh with a 1000-geodesic cache and 700 geo
 per file, and a SquareSubdivisionMeshV2 from a 17^2 seed, whose rounds depend on the
 values of the previous ones. Both kernels must reproduce every quadrant and pass count.
 """
+import os
+
+import numpy as np
 import pytest
 
 from foort_gb300 import abi, workloads
-from test_output import RUNS, compare_dirs
+from test_output import DAT, GEOPOS, RUNS, compare_dirs, geopos_workload
 
 pytestmark = pytest.mark.gpu
 
@@ -31,3 +34,62 @@ def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision):
     mesh.close()
     print(f"{name}: {geodesics} geodesics in {rounds} rounds")
     compare_dirs(tmp_path, name)
+
+
+def parse_geopos(path):
+    """{(row, col): (count, positions)} and the first line of a GeodesicPosition file."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    out = {}
+    order = []
+    for ln in lines[1:]:
+        head, tail = ln.split(" ;; ")
+        row, col, k = (int(x) for x in head.split())
+        out[(row, col)] = (k, np.array([float(x) for x in tail.split()]))
+        order.append((row, col))
+    return lines[0], out, order
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+@pytest.mark.parametrize("name", sorted(GEOPOS))
+def test_run_records_the_reference_positions(engine_lib, tmp_path, name, precision):
+    """GeodesicPosition through foort_gpu_run (two passes) against the strict reference:
+    same first line, same pixels, same number of kept positions, and positions equal to
+    the printed precision (FP64; the mixed kernel to its endpoint tolerance)."""
+    import foort_gb300
+    every, steps, val, spec = GEOPOS[name]
+    wl = geopos_workload(every, steps, val)
+    wl.desc.precision = precision
+    mesh = foort_gb300.Mesh.from_spec(spec, wl.desc.diag_flags, wl.desc.value_diag)
+    out = foort_gb300.Output(str(tmp_path / name), wl.desc.diag_flags, wl.desc.value_diag,
+                             first_line=mesh.first_line_info(wl.desc))
+    with foort_gb300.Engine(wl.desc) as e:
+        e.run([mesh], [out])
+    out.close()
+    mesh.close()
+    ref_first, ref, ref_order = parse_geopos(os.path.join(DAT, f"{name}_GeodesicPosition.dat"))
+    first, got, order = parse_geopos(str(tmp_path / f"{name}_GeodesicPosition.dat"))
+    assert first == ref_first
+    common = [p for p in ref_order if p in got]
+    if spec[0] == "v2":
+        # positions drive the mesh: near-equal weights may be ordered differently than
+        # in the reference's arithmetic (the mesh itself is pinned on the CPU against the
+        # strict oracle), so the runs are compared on the pixels they share
+        assert len(common) >= 0.95 * len(ref_order)
+        # The 17-wide grid has a row on the screen's alpha = 0 line (row 8): at 60 deg
+        # those rays pass over the rotation axis, where phi is singular, and the
+        # reference's own -Ofast and strict-IEEE builds already differ there (all 15 such
+        # rays of this run: other step counts, positions 1e-6 - 2e-5 apart, against 1e-9
+        # for the next row). They are left out of the comparison.
+        common = [p for p in common if p[0] != 8]
+    else:
+        assert order == ref_order
+    same = [p for p in common if got[p][0] == ref[p][0]]
+    assert len(same) >= (0.99 if precision == abi.PREC_FP64 else 0.95) * len(common), (len(same), len(common))
+    # per geodesic: do all its kept positions agree (relative, to the printed precision
+    # for FP64; to the mixed kernel's endpoint tolerance)?
+    tol = 2e-6 if precision == abi.PREC_FP64 else 1e-4
+    ok = np.array([np.all(np.abs(got[p][1] - ref[p][1]) <= tol * np.maximum(1.0, np.abs(ref[p][1]))) for p in same])
+    frac = 1.0 if precision == abi.PREC_FP64 else 0.99
+    print(f"{name}: {len(same)}/{len(ref_order)} same counts, {ok.mean():.5f} of those geodesics within {tol}")
+    assert ok.mean() >= frac

@@ -132,9 +132,11 @@ def test_writer_errors(engine_lib, tmp_path):
     with pytest.raises(foort_gb300.FoortError) as e:
         foort_gb300.Output("", abi.DIAG_FOUR_COLOR_SCREEN, abi.DIAG_FOUR_COLOR_SCREEN)
     assert e.value.code == abi.FOORT_E_UNSUPPORTED  # console output
-    with pytest.raises(foort_gb300.FoortError) as e:
-        foort_gb300.Output(str(tmp_path / "x"), abi.DIAG_GEODESIC_POSITION, abi.DIAG_GEODESIC_POSITION)
-    assert e.value.code == abi.FOORT_E_UNSUPPORTED
+    out = foort_gb300.Output(str(tmp_path / "x"), abi.DIAG_GEODESIC_POSITION, abi.DIAG_GEODESIC_POSITION)
+    with pytest.raises(foort_gb300.FoortError) as e:  # GeodesicPosition needs its positions
+        out.round(np.zeros(1, dtype=abi.PIXEL_DTYPE), np.zeros(1, dtype=abi.RESULT_DTYPE))
+    assert e.value.code == abi.FOORT_E_BADARG
+    out.close()
     blocker = tmp_path / "file"
     blocker.write_text("")
     out = foort_gb300.Output(str(blocker / "run"), abi.DIAG_FOUR_COLOR_SCREEN, abi.DIAG_FOUR_COLOR_SCREEN)
@@ -143,3 +145,97 @@ def test_writer_errors(engine_lib, tmp_path):
         out.finish()
     assert e.value.code == abi.FOORT_E_IO
     out.close()
+
+
+# ---- GeodesicPosition ---------------------------------------------------------------
+def geopos_workload(every, output_steps, value_geopos):
+    """The configuration of tests/golden/make_golden.py geopos_workload."""
+    wl = workloads.c2(abi.PREC_FP64)
+    d = wl.desc
+    d.diag_flags = abi.DIAG_GEODESIC_POSITION | (abi.DIAG_EQUATORIAL_PASSES if value_geopos else abi.DIAG_FOUR_COLOR_SCREEN)
+    d.value_diag = abi.DIAG_GEODESIC_POSITION if value_geopos else abi.DIAG_FOUR_COLOR_SCREEN
+    d.geopos_freq = abi.UpdateFreq(every, 0, 1)
+    d.geopos_output_steps = output_steps
+    return wl
+
+
+GEOPOS = {"geopos12": (1, 40, False, ("simple", 12)), "geopos12f3": (3, 25, True, ("simple", 12)),
+          "geoposv2": (1, 8, True, ("v2", dict(initial_pixels=81, max_subdivide=2, iteration_pixels=30)))}
+
+
+def read_geopos(name):
+    """(first line, px, counts, points) of a reference GeodesicPosition file."""
+    with open(os.path.join(DAT, f"{name}_GeodesicPosition.dat")) as f:
+        lines = f.read().splitlines()
+    px = np.zeros(len(lines) - 1, dtype=abi.PIXEL_DTYPE)
+    counts = np.zeros(len(px), dtype=np.uint64)
+    pts = []
+    for i, ln in enumerate(lines[1:]):
+        head, tail = ln.split(" ;; ")
+        row, col, k = (int(x) for x in head.split())
+        px["row"][i], px["col"][i], counts[i] = row, col, k
+        vals = [float(x) for x in tail.split()]
+        assert len(vals) == 4 * k
+        pts.append(np.array(vals).reshape(-1, 4))
+    return lines[0], px, counts, np.concatenate(pts)
+
+
+def test_geopos_counts_follow_the_step_counts(oracle_mod, engine_lib):
+    """Kept positions per geodesic from its step count (foort_geopos_count) against the
+    reference's files; the steps come from the strict oracle, which retraces the strict
+    reference the files were written with."""
+    import ctypes as C
+    for name in ("geopos12", "geopos12f3"):
+        every, steps, val, mesh = GEOPOS[name]
+        wl = geopos_workload(every, steps, val)
+        _, px, counts, _ = read_geopos(name)
+        px["grid"] = mesh[1]
+        res = oracle_mod.integrate(wl.desc, px, fast=False)
+        for i in range(len(px)):
+            s, k = C.c_uint64(), C.c_uint64()
+            assert engine_lib.foort_geopos_count(C.byref(wl.desc), int(res["steps"][i]), int(res["term"][i]),
+                                                 C.byref(s), C.byref(k)) == 0
+            assert k.value == counts[i], (name, i, int(res["steps"][i]), k.value, counts[i])
+
+
+@pytest.mark.parametrize("name", sorted(GEOPOS))
+def test_writer_reproduces_reference_geopos_files(engine_lib, tmp_path, name):
+    import foort_gb300
+    every, steps, val, _ = GEOPOS[name]
+    wl = geopos_workload(every, steps, val)
+    first, px, counts, points = read_geopos(name)
+    other = "EquatPasses" if val else "FourColorScreen"
+    _, vals = read_files(name, other)
+    assert (vals[:, 0] == px["row"]).all() and (vals[:, 1] == px["col"]).all()
+    res = np.zeros(len(px), dtype=abi.RESULT_DTYPE)
+    res["equat_passes" if val else "quadrant"] = vals[:, 2]
+    with foort_gb300.Output(str(tmp_path / name), wl.desc.diag_flags, wl.desc.value_diag, first_line=first) as out:
+        out.round(px, res, counts, points)
+        out.finish()
+    compare_dirs(tmp_path, name)
+
+
+def test_v2_mesh_driven_by_positions_follows_the_reference(oracle_mod, engine_lib):
+    """SquareSubdivisionMeshV2 with GeodesicPosition as its value diagnostic: the mesh
+    driven by the strict oracle's final (theta, phi) (the last position, which the
+    reference's getFinalDataVal returns at UpdateFrequency 1) hands out exactly the
+    reference's pixels, round after round. The great-circle distances are continuous, so
+    arithmetic that differs in the last bits may order near-equal weights differently:
+    the GPU tests compare such runs pixel by pixel instead."""
+    import ctypes as C
+    import foort_gb300
+    every, steps, val, spec = GEOPOS["geoposv2"]
+    wl = geopos_workload(every, steps, val)
+    m = foort_gb300.Mesh.from_spec(spec, wl.desc.diag_flags, wl.desc.value_diag)
+    order = []
+    while not m.finished():
+        px = m.pixels()
+        res = oracle_mod.integrate(wl.desc, px, fast=False)
+        for i in range(len(px)):
+            v = (C.c_double * 2)(res["pos"][i][2], res["pos"][i][3])
+            assert m._lib.foort_mesh_geodesic_finished(m._m, i, v, 2) == 0
+        m.end_round()
+        order += list(zip(px["row"].tolist(), px["col"].tolist()))
+    m.close()
+    _, ref_px, _, _ = read_geopos("geoposv2")
+    assert order == list(zip(ref_px["row"].tolist(), ref_px["col"].tolist()))
