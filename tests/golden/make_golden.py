@@ -182,6 +182,8 @@ def main(parts):
     oracle.build(with_ref=True)
     if "geopos" in parts:
         geopos_runs()
+    if "c5" in parts or "ref" in parts:
+        ref_case("c5", workloads.c5(abi.PREC_FP64), sample_pixels(4097, 300, 6))
     if "mesh" in parts:
         mesh_traces()
         first_lines()

@@ -58,7 +58,7 @@ def test_fp64_reproduces_shipped_golden(eng, oracle_mod, name):
 
 
 def _fixture_case(case):
-    wl = {"c1": workloads.c1, "c2": workloads.c2, "c4": workloads.c4,
+    wl = {"c1": workloads.c1, "c2": workloads.c2, "c4": workloads.c4, "c5": workloads.c5,
           "debug_sample": lambda: workloads.johannsen_golden(False),
           "c3": lambda: workloads.c3(precision=abi.PREC_FP64)}[case]()
     if case in ("c2", "c4"):
@@ -67,7 +67,7 @@ def _fixture_case(case):
     return wl
 
 
-@pytest.mark.parametrize("case", ["c1", "c2", "c3", "c4", "debug_sample"])
+@pytest.mark.parametrize("case", ["c1", "c2", "c3", "c4", "c5", "debug_sample"])
 def test_fp64_vs_reference_fixture(eng, oracle_mod, case):
     f = np.load(os.path.join(GOLDEN, f"ref_{case}.npz"))
     wl = _fixture_case(case)

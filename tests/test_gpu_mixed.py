@@ -64,7 +64,8 @@ def test_mixed_reproduces_shipped_golden(eng, oracle_mod, name, options):
 
 
 CASES = {"c1": lambda: workloads.c1(), "c2": lambda: workloads.c2(), "c3": lambda: workloads.c3(n_images=64),
-         "c4": lambda: workloads.c4(), "debug_sample": lambda: workloads.johannsen_golden(False)}
+         "c4": lambda: workloads.c4(), "c5": lambda: workloads.c5(),
+         "debug_sample": lambda: workloads.johannsen_golden(False)}
 
 
 @pytest.mark.parametrize("case", sorted(CASES))

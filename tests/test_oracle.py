@@ -29,7 +29,7 @@ def test_oracle_reproduces_shipped_dat(oracle_mod, name, fast):
     assert np.array_equal(res["equat_passes"], g["passes"].astype(np.int32))
 
 
-@pytest.mark.parametrize("case", ["c1", "c2", "c3", "c4", "debug_sample"])
+@pytest.mark.parametrize("case", ["c1", "c2", "c3", "c4", "c5", "debug_sample"])
 def test_oracle_bit_exact_vs_reference_strict(oracle_mod, case):
     f = np.load(os.path.join(GOLDEN, f"ref_{case}.npz"))
     wl = _workload(case)
@@ -41,7 +41,7 @@ def test_oracle_bit_exact_vs_reference_strict(oracle_mod, case):
         assert np.array_equal(res[k], ref[k]), k
 
 
-@pytest.mark.parametrize("case", ["c1", "c2", "c3", "c4", "debug_sample"])
+@pytest.mark.parametrize("case", ["c1", "c2", "c3", "c4", "c5", "debug_sample"])
 def test_oracle_fast_vs_reference_fast(oracle_mod, case):
     f = np.load(os.path.join(GOLDEN, f"ref_{case}.npz"))
     wl = _workload(case)
@@ -64,6 +64,8 @@ def _workload(case):
         wl = workloads.c4()
         wl.desc.value_diag = abi.DIAG_CLOSEST_RADIUS
         return wl
+    if case == "c5":
+        return workloads.c5()
     if case == "debug_sample":
         return workloads.johannsen_golden(False)
     raise KeyError(case)
