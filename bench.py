@@ -19,7 +19,8 @@ N > 1 (torchrun): every rank integrates its own copy of the workload (weak scali
 no collective on the data path); times are the max over ranks.
 --impl reference: the reference's algorithm on the host cores (the oracle's
 restatement built with the reference's -Ofast flags; the reference itself only builds
-where its sources are), on a bounded seeded sample of the workload's grid.
+where its sources are), on a bounded seeded sample of the pixels the reference's own
+complete C2 run integrates (tests/golden/c2_run.npz; other workloads: of their grid).
 """
 import argparse
 import json
@@ -196,6 +197,21 @@ def cpu_sample_rate(wl, px_all, target_seconds, nthreads, use_ref=False):
     return n / dt, n, dt, res
 
 
+def reference_run_pixels(args):
+    """The pixels of the reference's own complete C2 run (tests/golden/c2_run.npz:
+    26,547 pixels of the 509^2 grid, in its order) when the workload is C2 with its
+    default IterationPixels; None otherwise."""
+    from foort_gb300 import abi, workloads
+    fn = os.path.join(ROOT, "tests", "golden", "c2_run.npz")
+    if args.workload != "c2" or args.iteration_pixels not in (None, workloads.C2_ITERATION_PIXELS) \
+            or not os.path.exists(fn):
+        return None
+    f = np.load(fn)
+    px = np.zeros(len(f["row"]), dtype=abi.PIXEL_DTYPE)
+    px["row"], px["col"], px["grid"] = f["row"], f["col"], 509
+    return px
+
+
 def run_reference(args, rank):
     """--impl reference: the reference's algorithm on the host cores."""
     if rank != 0:
@@ -210,7 +226,11 @@ def run_reference(args, rank):
         side = spec
     else:
         side = int((math.sqrt(spec["initial_pixels"]) - 1) * 2 ** (spec["max_subdivide"] - 1) + 1)
-    grid = abi.square_pixels(side)
+    grid = reference_run_pixels(args)
+    where = f"of the reference's own complete run ({len(grid)} pixels of the {side}^2 grid)" if grid is not None \
+        else f"of the {side}^2 grid"
+    if grid is None:
+        grid = abi.square_pixels(side)
     nthreads = os.cpu_count() or 1
     per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
     use_ref = oracle.have_ref()
@@ -227,7 +247,7 @@ def run_reference(args, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_block(wl, args, side=side),
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": nthreads, "kind": kind_name,
-                         "sample": f"{rates[-1][1]} seeded-uniform pixels of the {side}^2 grid per step; "
+                         "sample": f"{rates[-1][1]} seeded-random pixels {where} per step; "
                                    + ("the reference compiled from its sources with its own -Ofast -fopenmp flags"
                                       if use_ref else "the oracle's restatement built with the reference's "
                                                       "-Ofast -fopenmp flags")},

@@ -18,7 +18,9 @@ Outputs (.npz of numpy arrays, a few hundred KB in total):
 * mesh_traces.npz              SquareSubdivisionMeshV2 / SimpleSquareMesh pixel sequences
                                driven by synthetic values;
 * first_lines.json             Utilities::GetFirstLineInfoString for several runs;
-* dat/*.dat                    output files of small complete runs (GeodesicOutputHandler).
+* dat/*.dat                    output files of small complete runs (GeodesicOutputHandler);
+* c2_run.npz                   the reference's complete C2 run: pixel order, quadrant and
+                               closest radius of its 26,547 geodesics (part "c2run").
 """
 import ctypes as C
 import json
@@ -178,8 +180,49 @@ def geopos_runs():
         print("geopos run", name, n.value, "geodesics", nr.value, "rounds")
 
 
+def read_dat(fn):
+    """First line and (row, col, value text) rows of one reference output file."""
+    lines = open(fn).read().split("\n")
+    rows = [l.split() for l in lines[1:] if l.strip()]
+    return lines[0], rows
+
+
+def c2_run():
+    """The reference's complete C2 run (Kerr a = 0.99 at 60 deg, SquareSubdivisionMeshV2
+    from a 128^2 seed, MaxSubdivide 3, IterationPixels 800), the reference's own -Ofast
+    build on all host threads (about 8 minutes on 8 cores). c2_run.npz keeps the order
+    in which the run handed out its pixels, the quadrant and closest radius of each, and
+    the files' first line."""
+    lib = oracle.ref_lib()
+    wl = workloads.c2(abi.PREC_FP64)
+    spec = oracle.RefMeshSpec(1, 3, 0, 0, 128 * 128, workloads.C2_ITERATION_PIXELS, 0, 0)
+    tmp = os.path.join(HERE, "_c2run_tmp")
+    os.makedirs(tmp, exist_ok=True)
+    prefix = os.path.join(tmp, "c2")
+    n, nr, sec = C.c_uint64(), C.c_uint32(), C.c_double()
+    rc = lib.ref_run(C.byref(wl.desc), C.byref(spec), prefix.encode(), b"", b"dat", 1 << 40, 1 << 40, 1, 0,
+                     C.byref(n), C.byref(nr), C.byref(sec))
+    assert rc == 0
+    head_q, quad = read_dat(prefix + "_FourColorScreen.dat")
+    head_c, clos = read_dat(prefix + "_ClosestRadius.dat")
+    assert head_q == head_c and len(quad) == len(clos) == n.value
+    assert all(a[:2] == b[:2] for a, b in zip(quad, clos))
+    np.savez_compressed(os.path.join(HERE, "c2_run.npz"),
+                        row=np.array([int(t[0]) for t in quad], np.uint16),
+                        col=np.array([int(t[1]) for t in quad], np.uint16),
+                        quadrant=np.array([int(t[2]) for t in quad], np.int8),
+                        closest_r=np.array([float(t[2]) for t in clos]),
+                        rounds=np.array(nr.value), seconds=np.array(sec.value), header=np.array(head_q))
+    for f in os.listdir(tmp):
+        os.remove(os.path.join(tmp, f))
+    os.rmdir(tmp)
+    print("c2 run", n.value, "geodesics", nr.value, "rounds", f"{sec.value:.0f} s")
+
+
 def main(parts):
     oracle.build(with_ref=True)
+    if "c2run" in parts:
+        c2_run()
     if "geopos" in parts:
         geopos_runs()
     if "c5" in parts or "ref" in parts:

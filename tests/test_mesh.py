@@ -58,3 +58,40 @@ def test_value_vector_follows_the_rotated_diagnostic_order(engine_lib):
     m2.set_values([5.0] * len(px))
     m2.end_round()
     assert m1.size() > 0 and m2.size() == 0
+
+
+def c2_run_fixture():
+    """The reference's complete C2 run (tests/golden/c2_run.npz, make_golden.py part
+    "c2run"): per geodesic in hand-out order its pixel, quadrant and closest radius."""
+    f = np.load(os.path.join(GOLDEN, "c2_run.npz"))
+    return {k: f[k] for k in f.files}
+
+
+def test_v2_mesh_hands_out_the_reference_c2_run(engine_lib):
+    """Given the reference's own quadrant of every pixel, the host V2 mesh of the C2
+    workload (128^2 seed, MaxSubdivide 3, IterationPixels 800) hands out the reference
+    run's 26,547 pixels in the same order, over the same five rounds."""
+    import foort_gb300
+    from foort_gb300 import workloads
+    f = c2_run_fixture()
+    rows, cols = f["row"].astype(np.int64), f["col"].astype(np.int64)
+    wl = workloads.c2()
+    mesh = foort_gb300.Mesh.from_spec(wl.mesh[0], wl.desc.diag_flags, wl.desc.value_diag)
+    grid = mesh.grid()
+    assert grid == 509
+    quad = np.full((grid, grid), -1, np.int64)
+    quad[rows, cols] = f["quadrant"]
+    assert len(np.unique(rows * grid + cols)) == len(rows)  # every pixel once
+    k, r = 0, 0
+    while not mesh.finished():
+        px = mesh.pixels()
+        n = len(px)
+        assert np.array_equal(px["row"], rows[k:k + n]), r
+        assert np.array_equal(px["col"], cols[k:k + n]), r
+        mesh.set_values(quad[px["row"].astype(np.int64), px["col"].astype(np.int64)])
+        mesh.end_round()
+        k += n
+        r += 1
+    mesh.close()
+    assert k == len(rows) == 26547
+    assert r == int(f["rounds"]) == 5
