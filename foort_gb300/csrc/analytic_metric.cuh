@@ -9,6 +9,8 @@
 
 #include <math.h>
 
+#include <cmath>
+
 #include "gen_christoffel.inc"
 #include "metric_fp64.cuh"
 
@@ -96,6 +98,35 @@ struct MixedMetric {
 FOORT_DEFINE_MIXED_METRIC(kKerr, FOORT_MIXED_BODY_KERR, true)
 FOORT_DEFINE_MIXED_METRIC(kJohannsen, FOORT_MIXED_BODY_JOHANNSEN, false)
 FOORT_DEFINE_MIXED_METRIC(kFlat, FOORT_MIXED_BODY_FLAT, true)
+FOORT_DEFINE_MIXED_METRIC(kRasheedLarsen, FOORT_MIXED_BODY_RASHEEDLARSEN, false)
+
+// The plugins' constants q[]: the metric constants of make_metric_const for Kerr,
+// Johannsen and flat space; for Rasheed-Larsen the slots of its rewritten form
+// (gen_christoffel.py), from its rescaled m, a, p, q.
+inline void mixed_metric_constants(int id, const MetricConst& M, double out[kMixedQ]) {
+    for (int i = 0; i < kMixedQ; ++i) out[i] = 0.0;
+    if (id == kRasheedLarsen) {
+        const double a = M.q[0], m = M.q[1], p = M.q[2], qq = M.q[3];
+        FOORT_MIXED_CONSTANTS_RASHEEDLARSEN
+        return;
+    }
+    for (int i = 0; i < 6; ++i) out[i] = M.q[i];
+}
+
+// r_+ and r_- of the plugin's Delta = (r - r_+)(r - r_-) = r^2 - 2 m r + a^2: m = 1 for
+// Kerr and Johannsen, Rasheed-Larsen's rescaled m; none for flat space.
+inline void mixed_horizons(int id, const MetricConst& M, double& rp, double& rm) {
+    rp = rm = 0.0;
+    if (id == kKerr || id == kJohannsen) {
+        const double a = M.q[0];
+        rp = 1.0 + std::sqrt(1.0 - a * a);
+        rm = 1.0 - std::sqrt(1.0 - a * a);
+    } else if (id == kRasheedLarsen) {
+        const double a = M.q[0], m = M.q[1];
+        rp = m + std::sqrt(m * m - a * a);
+        rm = m - std::sqrt(m * m - a * a);
+    }
+}
 
 // d_x1 g and g^11 in log-r mode (x1 = ln r): d_x1 = r d_r, g_11 = r^2 g_rr,
 // g^11 = g^rr / r^2.

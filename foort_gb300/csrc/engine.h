@@ -14,7 +14,7 @@ constexpr double kRefPi = 3.1415926535;
 // Constants of the mixed-precision kernel (per image). Pairs [2] are float-float
 // (hi, lo) splits of a double; thresholds are in ln r in log-r mode.
 struct MixedConst {
-    float q[6];        // metric constants in FP32
+    float q[kMixedQ];  // analytic plugin constants in FP32 (ImageConst::qa)
     float rp[2];       // r_+ (Delta = (r - r_+)(r - r_-))
     float rm[2];       // r_-
     float lrp[2];      // ln r_+
@@ -43,6 +43,7 @@ struct ImageConst {
     double size[2];     // screen size
     double center[2];   // screen center
     double h_eps;       // Epsilon_Horizon of this image (relative)
+    double qa[kMixedQ]; // analytic plugin constants (mixed_metric_constants)
     MixedConst mx;
 };
 

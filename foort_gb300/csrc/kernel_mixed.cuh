@@ -316,7 +316,7 @@ struct MixedEngine {
                                                const float u[4], float a[4]) {
         const bool rlog = R.rlog != 0;
         if (I.mx.r_fp64 > 0.f && x1.hi < I.mx.r_fp64) {
-            rhs_fp64_path<MID>(I.m.q, I.mx, rlog, x1, th, u, a);
+            rhs_fp64_path<MID>(I.qa, I.mx, rlog, x1, th, u, a);
             ++L.fp64;
         } else if (MixedMetric<MID>::kInline) {
             rhs_analytic<MID, float>(I.mx.q, I.mx, rlog, x1, th, u, a);

@@ -29,6 +29,9 @@ struct MetricConst {
     double rh;    // horizon radius (0 for flat space)
 };
 
+// Number of constant slots of the analytic metric plugins (analytic_metric.cuh).
+constexpr int kMixedQ = 20;
+
 // Metric ids (include/foort_gpu.h FOORT_METRIC_*).
 enum MetricId { kKerr = 0, kFlat = 1, kRasheedLarsen = 2, kJohannsen = 3, kMankoNovikov = 4 };
 

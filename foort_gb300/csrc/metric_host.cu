@@ -12,16 +12,14 @@ namespace {
 template <int MID>
 int christoffel_host(const double* params, bool rlog, const double* x, double* gamma) {
     MetricConst M = make_metric_const(MID, params);
-    double rp = 0.0, rm = 0.0;
-    if (MID == kKerr || MID == kJohannsen) {
-        rp = 1.0 + std::sqrt(1.0 - params[0] * params[0]);
-        rm = 1.0 - std::sqrt(1.0 - params[0] * params[0]);
-    }
+    double q[kMixedQ], rp, rm;
+    mixed_metric_constants(MID, M, q);
+    mixed_horizons(MID, M, rp, rm);
     const double r = rlog ? std::exp(x[1]) : x[1];
     const double s = std::sin(x[2]), c = std::cos(x[2]);
     G5T<double> dr, dh, gu;
     double grr;
-    MixedMetric<MID>::template eval<double>(M.q, r, r - rp, r - rm, s, c, dr, dh, gu, grr);
+    MixedMetric<MID>::template eval<double>(q, r, r - rp, r - rm, s, c, dr, dh, gu, grr);
     if (rlog) to_log_r(r, grr, dr, dh, gu);
     double d[4][4][4] = {}, g[4][4] = {};
     auto put = [](double m[4][4], const G5T<double>& v) {
@@ -50,6 +48,7 @@ extern "C" int foort_metric_christoffel(int32_t metric_id, const double* params,
     case FOORT_METRIC_KERR: return christoffel_host<kKerr>(params, rlog != 0, x, gamma);
     case FOORT_METRIC_JOHANNSEN: return christoffel_host<kJohannsen>(params, rlog != 0, x, gamma);
     case FOORT_METRIC_FLAT: return christoffel_host<kFlat>(params, false, x, gamma);
+    case FOORT_METRIC_RASHEED_LARSEN: return christoffel_host<kRasheedLarsen>(params, rlog != 0, x, gamma);
     default: return FOORT_E_UNSUPPORTED;
     }
 }

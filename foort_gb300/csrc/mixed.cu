@@ -9,14 +9,16 @@ namespace foort {
 const void* mixed_kernel_kerr(int integrator, bool decide64);
 const void* mixed_kernel_joh(int integrator, bool decide64);
 const void* mixed_kernel_flat(int integrator, bool decide64);
+const void* mixed_kernel_rl(int integrator, bool decide64);
 
 // Mixed kernels exist for the metrics with analytic derivatives (gen_christoffel.py);
-// Rasheed-Larsen and Manko-Novikov run in FP64 only.
+// Manko-Novikov runs in FP64 only.
 const void* mixed_kernel_variant(int metric_id, int integ, bool decide64) {
     switch (metric_id) {
     case kKerr: return mixed_kernel_kerr(integ, decide64);
     case kJohannsen: return mixed_kernel_joh(integ, decide64);
     case kFlat: return mixed_kernel_flat(integ, decide64);
+    case kRasheedLarsen: return mixed_kernel_rl(integ, decide64);
     default: return nullptr;
     }
 }
@@ -38,13 +40,10 @@ const void* mixed_pair_kernel_variant(int metric_id, int integ, bool decide64) {
 
 void fill_mixed_constants(int metric_id, ImageConst& ic, const RunConst& rc) {
     MixedConst& mx = ic.mx;
-    for (int i = 0; i < 6; ++i) mx.q[i] = static_cast<float>(ic.m.q[i]);
-    double rp = 0.0, rm = 0.0;
-    if (metric_id == kKerr || metric_id == kJohannsen) {
-        const double a = ic.m.q[0];
-        rp = 1.0 + std::sqrt(1.0 - a * a);
-        rm = 1.0 - std::sqrt(1.0 - a * a);
-    }
+    mixed_metric_constants(metric_id, ic.m, ic.qa);
+    for (int i = 0; i < kMixedQ; ++i) mx.q[i] = static_cast<float>(ic.qa[i]);
+    double rp, rm;
+    mixed_horizons(metric_id, ic.m, rp, rm);
     mx.rpv = rp;
     mx.rmv = rm;
     ff_split(rp, mx.rp[0], mx.rp[1]);

@@ -20,13 +20,11 @@ using namespace foort;
 template <int MID>
 void run(const char* name, const double* params, bool rlog) {
     MetricConst M = make_metric_const(MID, params);
-    double rp = 0.0, rm = 0.0;
-    if (MID == kKerr || MID == kJohannsen) {
-        rp = 1.0 + std::sqrt(1.0 - params[0] * params[0]);
-        rm = 1.0 - std::sqrt(1.0 - params[0] * params[0]);
-    }
-    float qf[6];
-    for (int i = 0; i < 6; ++i) qf[i] = static_cast<float>(M.q[i]);
+    double qd[kMixedQ], rp, rm;
+    mixed_metric_constants(MID, M, qd);
+    mixed_horizons(MID, M, rp, rm);
+    float qf[kMixedQ];
+    for (int i = 0; i < kMixedQ; ++i) qf[i] = static_cast<float>(qd[i]);
     std::mt19937_64 rng(7);
     std::uniform_real_distribution<double> U(0.0, 1.0);
     std::vector<double> errs;
@@ -37,7 +35,7 @@ void run(const char* name, const double* params, bool rlog) {
         const double s = std::sin(th), c = std::cos(th);
         G5T<double> dr, dh, gu;
         double grr;
-        MixedMetric<MID>::template eval<double>(M.q, r, r - rp, r - rm, s, c, dr, dh, gu, grr);
+        MixedMetric<MID>::template eval<double>(qd, r, r - rp, r - rm, s, c, dr, dh, gu, grr);
         G5 g = metric_dd_host(MID, M, r, s, c, false);
         // random spatial direction, u^t from the null condition with E = -u_t ~ 1
         double ur = 2 * U(rng) - 1, uh = (2 * U(rng) - 1) / r, up = (2 * U(rng) - 1) / (r * (s + 1e-3));
@@ -124,5 +122,15 @@ int main() {
     run<kJohannsen>("johannsen_test_logr", joh_test, true);
     run<kJohannsen>("johannsen_all_params", joh_all, false);
     run<kFlat>("flat", none, false);
+    // Rasheed-Larsen: the "Lorenzo" and "M1" parameter sets of the reference's Test.cfg
+    // (M1 is extremal, m = a), and the reference's defaults (p = 2m: no dyonic terms)
+    const double rl_lorenzo[6] = {0.3556562853309941, 0.2969060968239216, 3.057664971085168, 0.942335028914832};
+    const double rl_m1[6] = {0.0000292676523070559347272298622578, 0.0000292676523070559347272298622578,
+                             3.15470053516341633378322799917, 0.84529946483658456162619604143};
+    const double rl_default[6] = {1.0, 0.5, 2.0, 2.0};
+    run<kRasheedLarsen>("rasheed_larsen_lorenzo", rl_lorenzo, false);
+    run<kRasheedLarsen>("rasheed_larsen_lorenzo_logr", rl_lorenzo, true);
+    run<kRasheedLarsen>("rasheed_larsen_m1", rl_m1, false);
+    run<kRasheedLarsen>("rasheed_larsen_default", rl_default, false);
     return 0;
 }

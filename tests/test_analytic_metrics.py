@@ -4,7 +4,9 @@
   (Metric.cpp:14-55, restated by the oracle) to the finite differences' own accuracy.
 * In FP32 (tests/analytic_check.cpp, the same plugin code the kernel runs) the
   geodesic acceleration must keep FP32 accuracy from r_+ + 0.01 to 1000: no overflow
-  (Johannsen's expanded numerators would reach r^15) and no near-horizon cancellation.
+  (Johannsen's expanded numerators would reach r^15), no near-horizon cancellation, and
+  for Rasheed-Larsen none on its ergosurface (H3 = 0) or, with near-extremal
+  parameters, at small r.
 """
 import ctypes as C
 import os
@@ -15,8 +17,14 @@ import pytest
 
 from conftest import ROOT
 
+# Rasheed-Larsen: the "Lorenzo" and extremal "M1" parameter sets of the reference's
+# Test.cfg, and its defaults (m, a, p, q)
+RL_LORENZO = (0.3556562853309941, 0.2969060968239216, 3.057664971085168, 0.942335028914832)
+RL_M1 = (0.0000292676523070559347272298622578, 0.0000292676523070559347272298622578,
+         3.15470053516341633378322799917, 0.84529946483658456162619604143)
 CASES = [(0, (0.99,), 0), (0, (0.7,), 1), (3, (0.9, -0.6, 0, 0, 0), 0), (3, (0.7, 2.0, 0, 0, 0), 1),
-         (3, (0.8, 1.0, 0.5, 0.2, 0.1), 0), (1, (), 0)]
+         (3, (0.8, 1.0, 0.5, 0.2, 0.1), 0), (1, (), 0), (2, RL_LORENZO, 0), (2, RL_LORENZO, 1), (2, RL_M1, 0),
+         (2, (1.0, 0.5, 2.0, 2.0), 0)]
 
 
 @pytest.mark.parametrize("metric,params,rlog", CASES)
@@ -37,7 +45,7 @@ def test_analytic_christoffel_equals_finite_differences(engine_lib, oracle_mod, 
     assert worst < 1e-7, worst
 
 
-def test_no_analytic_plugin_for_rasheed_larsen_and_manko_novikov(engine_lib):
+def test_no_analytic_plugin_for_manko_novikov(engine_lib):
     p = np.array([0.94, 13.0, 0, 0, 0, 0.0])
     x = np.array([0.0, 10.0, 1.0, 0.0])
     g = np.zeros(64)

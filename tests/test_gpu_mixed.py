@@ -132,6 +132,43 @@ def test_two_lanes_per_geodesic_give_the_one_lane_results(eng, case):
         np.testing.assert_array_equal(out[0][name], out[1][name], err_msg=name)
 
 
+# Rasheed-Larsen parameter sets (m, a, p, q): "Lorenzo" and the extremal "M1" of the
+# reference's Test.cfg, and the reference's defaults
+RL_SETS = {"lorenzo": (0.3556562853309941, 0.2969060968239216, 3.057664971085168, 0.942335028914832),
+           "m1": (0.0000292676523070559347272298622578, 0.0000292676523070559347272298622578,
+                  3.15470053516341633378322799917, 0.84529946483658456162619604143),
+           "default": (1.0, 0.5, 2.0, 2.0)}
+
+
+@pytest.mark.parametrize("name,rlog,integ", [("lorenzo", 0, abi.INTEGRATOR_RK4), ("lorenzo", 1, abi.INTEGRATOR_RK4),
+                                             ("m1", 0, abi.INTEGRATOR_RK4), ("default", 0, abi.INTEGRATOR_RK4),
+                                             ("lorenzo", 0, abi.INTEGRATOR_VERLET)])
+def test_mixed_rasheed_larsen(eng, oracle_mod, name, rlog, integ):
+    """Rasheed-Larsen seen at 63 deg on a 48^2 screen: the mixed kernel's discrete
+    outcomes against the FP64 kernel (disagreements explained by the oracle), and its
+    endpoint error against the FP64 kernel within the mixed tolerances."""
+    d = workloads.base_desc()
+    d.metric_id, d.rlog, d.integrator_id = abi.METRIC_RASHEED_LARSEN, rlog, integ
+    d.term_flags |= abi.TERM_THETA_SINGULARITY
+    d.timeout_max_steps = 20000
+    d.diag_flags = abi.DIAG_FOUR_COLOR_SCREEN | abi.DIAG_EQUATORIAL_PASSES | abi.DIAG_CLOSEST_RADIUS
+    keep = abi.attach_images(d, [abi.make_image(RL_SETS[name], r=1000.0, theta=1.1, half_width=12.0)])
+    px = abi.square_pixels(48)
+    res, sm = run(eng, d, px, abi.PREC_MIXED)
+    r64, s64 = run(eng, d, px, abi.PREC_FP64)
+    d.precision = abi.PREC_FP64
+    mism = parity.discrete_mismatch(res, r64)
+    unexplained = parity.explain_mismatches(oracle_mod, d, px, res, mism)
+    same = (~mism) & (res["steps"] == r64["steps"])
+    s = parity.summarize(parity.endpoint_rel_err(res[same], r64[same], rlog=bool(rlog)))
+    print(f"RL {name} rlog={rlog} integrator={integ}: agreement {1 - mism.mean():.4f}, same steps "
+          f"{same.mean():.4f}, endpoint {s}, speed-up {s64['kernel_ms'] / sm['kernel_ms']:.1f}x")
+    assert len(unexplained) == 0, unexplained
+    assert 1 - mism.mean() >= parity.MIN_DISCRETE_AGREEMENT
+    assert s["median"] < MIXED_MEDIAN_TOL and s["p90"] < MIXED_P90_TOL, s
+    del keep
+
+
 def test_mixed_budget_and_cancel_paths(eng):
     wl = workloads.c1(precision=abi.PREC_MIXED)
     px = abi.square_pixels(60)
