@@ -232,7 +232,9 @@ def run_reference(args, rank):
     if grid is None:
         grid = abi.square_pixels(side)
     nthreads = os.cpu_count() or 1
-    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    # a few seconds of all host threads per step: shorter samples measure the one
+    # slowest geodesic of the sample more than the throughput
+    per_step = max(4.0, (args.cpu_seconds or 40.0) / max(1, args.steps + args.warmup))
     use_ref = oracle.have_ref()
     kind_name = "reference" if use_ref else "port"
     rates = []
@@ -322,7 +324,8 @@ def main():
     ap.add_argument("--iteration-pixels", type=int, default=None)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=None,
+                    help="host-core seconds of the CPU legs (default: 15 for cpu_baseline, 40 for --impl reference)")
     ap.add_argument("--profile-precision", default="both", choices=["both", "mixed", "fp64"])
     ap.add_argument("--lanes", type=int, default=0, choices=[0, 1, 2],
                     help="lanes per geodesic of the mixed kernel: 0 chosen per launch (default), 1 or 2")
@@ -507,7 +510,7 @@ def main():
     if not args.no_cpu and rank == 0:
         nthreads = os.cpu_count() or 1
         wl_cpu = workload(args.workload, abi.PREC_FP64, args.iteration_pixels)
-        rate, n, dt, _ = cpu_sample_rate(wl_cpu, np.concatenate(rounds), args.cpu_seconds, nthreads)
+        rate, n, dt, _ = cpu_sample_rate(wl_cpu, np.concatenate(rounds), args.cpu_seconds or 15.0, nthreads)
         cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
                "sample": f"{n} seeded-random pixels of this run's pixel set, {dt:.1f} s; oracle restatement "
                          f"built with the reference's -Ofast -fopenmp flags"}
