@@ -12,9 +12,14 @@
 
 namespace foort {
 
+// The position-dependent part of the right-hand side: central differences of g_dd in x1
+// and x2 and the inverse metric at x (Metric.cpp:14-38).
+struct FdParts {
+    G5 dr, dh, gu;
+};
+
 template <int MID>
-__device__ __forceinline__ void rhs_fd_fp64(const MetricConst& M, bool rlog, double hfd, const double x[4],
-                                            const double v[4], double acc[4]) {
+__device__ __forceinline__ FdParts fd_parts_fp64(const MetricConst& M, bool rlog, double hfd, const double x[4]) {
     using Mt = MetricFP64<MID>;
     double r0, rp, rm;
     if (rlog) {
@@ -36,12 +41,30 @@ __device__ __forceinline__ void rhs_fd_fp64(const MetricConst& M, bool rlog, dou
     const G5 d = Mt::dd(M, r0, sm, cm, rlog);
     const G5 gu = Mt::uu(M, r0, s0, c0, rlog);
     const double inv = 1 / (2 * hfd);
-    G5 dr, dh;
+    FdParts P;
+    G5& dr = P.dr;
+    G5& dh = P.dh;
     dr.tt = (a.tt - b.tt) * inv; dr.tp = (a.tp - b.tp) * inv; dr.rr = (a.rr - b.rr) * inv;
     dr.hh = (a.hh - b.hh) * inv; dr.pp = (a.pp - b.pp) * inv;
     dh.tt = (c.tt - d.tt) * inv; dh.tp = (c.tp - d.tp) * inv; dh.rr = (c.rr - d.rr) * inv;
     dh.hh = (c.hh - d.hh) * inv; dh.pp = (c.pp - d.pp) * inv;
+    P.gu = gu;
+    return P;
+}
+
+// The Christoffel symbols from the parts and their contraction with v (Metric.cpp:39-53,
+// Integrators.cpp:60-68).
+__device__ __forceinline__ void contract_fp64(const FdParts& P, const double v[4], double acc[4]) {
+    const G5& dr = P.dr;
+    const G5& dh = P.dh;
+    const G5& gu = P.gu;
 #include "gen_fd_christoffel.inc"
+}
+
+template <int MID>
+__device__ __forceinline__ void rhs_fd_fp64(const MetricConst& M, bool rlog, double hfd, const double x[4],
+                                            const double v[4], double acc[4]) {
+    contract_fp64(fd_parts_fp64<MID>(M, rlog, hfd, x), v, acc);
 }
 
 // Integrators::GetAdaptiveStep, Integrators.cpp:34-46
@@ -68,10 +91,12 @@ struct Fp64Engine {
         uint32_t fp64 = 0;
         int32_t term = 0;
         GeoposRec gp;  // set by the loop before init
+        FdParts P;     // Verlet: the parts at x (computed at the previous step's new position)
     };
 
     static __device__ __forceinline__ void init(Lane& L, const ImageConst& I, const RunConst& R, const foort_pixel& p) {
         initial_conditions(I, p, L.x, L.v);
+        if (INTEG == FOORT_INTEGRATOR_VERLET) L.P = fd_parts_fp64<MID>(I.m, R.rlog != 0, R.hfd, L.x);
         L.lam = 0.0;
         L.steps = 0;
         L.err = 0;
@@ -108,15 +133,20 @@ struct Fp64Engine {
             }
             L.rhs += 4;
         } else {  // Integrators.cpp:99-152
+            // Every right-hand side after the first is evaluated at the new position nx,
+            // which is where the next step's first one is evaluated: the metric parts
+            // there are computed once and kept for the next step. The reference computes
+            // them again from the same nx, so the values are the same.
             double a0[4], a1[4], vi[4];
-            rhs_fd_fp64<MID>(M, rlog, R.hfd, L.x, L.v, a0);
+            contract_fp64(L.P, L.v, a0);
             const double hh2 = h * h / 2.0;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 nx[i] = (L.x[i] + L.v[i] * h) + a0[i] * hh2;
                 vi[i] = L.v[i] + a0[i] * h;
             }
-            rhs_fd_fp64<MID>(M, rlog, R.hfd, nx, vi, a1);
+            const FdParts Pn = fd_parts_fp64<MID>(M, rlog, R.hfd, nx);
+            contract_fp64(Pn, vi, a1);
             const double h2 = h / 2.0;
 #pragma unroll
             for (int i = 0; i < 4; ++i) nv[i] = L.v[i] + (a0[i] + a1[i]) * h2;
@@ -138,12 +168,13 @@ struct Fp64Engine {
                     }
 #pragma unroll
                     for (int i = 0; i < 4; ++i) vi[i] = nv[i];
-                    rhs_fd_fp64<MID>(M, rlog, R.hfd, nx, vi, a1);
+                    contract_fp64(Pn, vi, a1);
 #pragma unroll
                     for (int i = 0; i < 4; ++i) nv[i] = L.v[i] + (a0[i] + a1[i]) * h2;
                     L.rhs += 1;
                 }
             }
+            L.P = Pn;
         }
         L.lam += h;
 #pragma unroll

@@ -145,6 +145,13 @@ __device__ __noinline__ F4 rhs_f32_called(const float* q, const MixedConst& mc, 
     return F4{a[0], a[1], a[2], a[3]};
 }
 
+// The called form of the FP32 metric part (Verlet keeps it from step to step).
+template <int MID>
+__device__ __noinline__ MetricAt<float> metric_part_called(const float* q, const MixedConst& mc, bool rlog, ff x1,
+                                                           ff th) {
+    return metric_part<MID, float>(q, mc, rlog, x1, th);
+}
+
 template <int MID>
 __device__ __noinline__ void rhs_fp64_path(const double* q, const MixedConst& mc, bool rlog, ff x1, ff th,
                                            const float uf[4], float a[4]) {
@@ -195,7 +202,23 @@ struct MixedEngine {
         uint32_t fp64 = 0;
         int32_t term = 0;
         GeoposRec gp;  // set by the loop before init
+        MetricAt<float> mc;  // Verlet: the metric part at the current (x1, theta)
     };
+
+    // Verlet keeps the metric part from step to step unless lanes may switch to the FP64
+    // right-hand side near the horizon.
+    static __device__ __forceinline__ bool verlet_cached(const ImageConst& I) {
+        return INTEG == FOORT_INTEGRATOR_VERLET && !(I.mx.r_fp64 > 0.f);
+    }
+
+    // The FP32 metric part at (x1, theta): inlined for the inlined plugins, called otherwise.
+    static __device__ __forceinline__ MetricAt<float> metric(const ImageConst& I, bool rlog, ff x1, ff th) {
+        if constexpr (MixedMetric<MID>::kInline) {
+            return metric_part<MID, float>(I.mx.q, I.mx, rlog, x1, th);
+        } else {
+            return metric_part_called<MID>(I.mx.q, I.mx, rlog, x1, th);
+        }
+    }
 
     // GeodesicPosition sample of the compensated position (second pass only)
     static __device__ __forceinline__ void geopos(Lane& L, const RunConst& R, double lam) {
@@ -233,6 +256,7 @@ struct MixedEngine {
         L.has_rmin = false;
         L.T.cH = L.T.cB = L.T.cT = L.T.cTh = 0;
         L.T.tcur = 0;
+        if (verlet_cached(I)) L.mc = metric(I, R.rlog != 0, L.x[1], L.x[2]);
         diags(L, I, R, true);  // Geodesic::Reset's start sample at lambda = 0
         if (L.gp.dst) geopos(L, R, 0.0);
     }
@@ -382,6 +406,8 @@ struct MixedEngine {
             }
             rk4_combine(h, k1, k2, k3, k4, du, dxc);
             L.rhs += 4;
+        } else if (verlet_cached(I)) {
+            return step_verlet_cached(L, I, R, h, uf);
         } else {
             // velocity Verlet (Integrators.cpp:99-152); the velocity change of each
             // iteration is formed as h/2 (a1_new - a1_old), free of cancellation.
@@ -434,6 +460,65 @@ struct MixedEngine {
             }
         }
         return advance(L, I, R, h, du, dxc);
+    }
+
+    // Velocity Verlet (Integrators.cpp:99-152) with one metric part per step. Every
+    // right-hand side after the first is evaluated at the new position (x1n, thn), which
+    // is where the next step's first one is evaluated: its metric part is computed once,
+    // used for the new acceleration and every velocity iteration, and kept for the next
+    // step. The new position's x1 and theta are stored as the metric saw them.
+    static __device__ __forceinline__ bool step_verlet_cached(Lane& L, const ImageConst& I, const RunConst& R, float h,
+                                                              const float uf[4]) {
+        const bool rlog = R.rlog != 0;
+        float a0[4], a1[4], vi[4], du[4], dxc[4];
+        accel_part(L.mc, rlog, uf, a0);
+        const float hh2 = 0.5f * h * h;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            dxc[i] = hh2 * a0[i];
+            vi[i] = uf[i] + h * a0[i];
+        }
+        const ff x1n = ff_add_f(ff_add(L.x[1], two_prod(h, L.v[1].hi)), __fmaf_rn(h, L.v[1].lo, dxc[1]));
+        const ff thn = ff_add_f(ff_add(L.x[2], two_prod(h, L.v[2].hi)), __fmaf_rn(h, L.v[2].lo, dxc[2]));
+        const MetricAt<float> mn = metric(I, rlog, x1n, thn);
+        accel_part(mn, rlog, vi, a1);
+        L.rhs += 2;
+        const float h2 = 0.5f * h;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) du[i] = h2 * (a0[i] + a1[i]);
+        if (R.vtol > 0.0) {
+            const float tol2 = static_cast<float>(R.vtol * R.vtol);
+            float dv[4];  // first correction: nv - vi = h/2 (a1 - a0)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) dv[i] = h2 * (a1[i] - a0[i]);
+            for (int it = 0;; ++it) {
+                float num = 0.f, den = 0.f;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float nvi = uf[i] + du[i];
+                    num += dv[i] * dv[i];
+                    den += nvi * nvi;
+                }
+                if (!(num > tol2 * den)) break;
+                if (it >= R.verlet_cap) {
+                    L.err |= FOORT_ERR_VERLET_ITER;
+                    break;
+                }
+                float a1n[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) vi[i] = uf[i] + du[i];
+                accel_part(mn, rlog, vi, a1n);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    dv[i] = h2 * (a1n[i] - a1[i]);
+                    a1[i] = a1n[i];
+                    du[i] = h2 * (a0[i] + a1[i]);
+                }
+                L.rhs += 1;
+            }
+        }
+        L.mc = mn;
+        return advance(L, I, R, h, du, dxc, &x1n, &thn);
     }
 
     // RK4's velocity increment du = h/6 (k1 + 2 k2 + 2 k3 + k4) and the O(h^2) part of the
@@ -505,14 +590,20 @@ struct MixedEngine {
 
     // The end of a step: x += h u + dxc; u += du; lambda += h; terminations; diagnostics.
     static __device__ __forceinline__ bool advance(Lane& L, const ImageConst& I, const RunConst& R, float h,
-                                                   const float du[4], const float dxc[4]) {
+                                                   const float du[4], const float dxc[4], const ff* x1n = nullptr,
+                                                   const ff* thn = nullptr) {
         // The increments are rounded to one float each (relative error 6e-8 of a step's
         // change, unbiased, so it accumulates as a random walk); what the float-float sum
         // prevents is the absorption of small increments into the large coordinate.
+        // x1n / thn: the new x1 and theta where the caller already formed them.
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             L.x[i] = ff_add_f(L.x[i], __fmaf_rn(h, L.v[i].hi, dxc[i]));
             L.v[i] = ff_add_f(L.v[i], du[i]);
+        }
+        if (x1n) {
+            L.x[1] = *x1n;
+            L.x[2] = *thn;
         }
         L.lam = ff_add_f(L.lam, h);
         ++L.steps;
