@@ -336,12 +336,14 @@ struct MixedEngine {
         return FOORT_TERMCODE_CONTINUE;
     }
 
-    static __device__ __forceinline__ void rhs(const ImageConst& I, const RunConst& R, Lane& L, ff x1, ff th,
+    // A right-hand side through the plugin's FP32 form (inlined or called) or, inside
+    // r_+ + margin when that option is on, the FP64 one; fp64 counts the latter.
+    static __device__ __forceinline__ void rhs(const ImageConst& I, const RunConst& R, uint32_t& fp64, ff x1, ff th,
                                                const float u[4], float a[4]) {
         const bool rlog = R.rlog != 0;
         if (I.mx.r_fp64 > 0.f && x1.hi < I.mx.r_fp64) {
             rhs_fp64_path<MID>(I.qa, I.mx, rlog, x1, th, u, a);
-            ++L.fp64;
+            ++fp64;
         } else if (MixedMetric<MID>::kInline) {
             rhs_analytic<MID, float>(I.mx.q, I.mx, rlog, x1, th, u, a);
         } else {
@@ -353,113 +355,140 @@ struct MixedEngine {
         }
     }
 
+    // One Geodesic::Update (Geodesic.cpp:61-88) through the integrator's step. The
+    // common cases run inline: RK4 with an inlined plugin (stages reordered) and Verlet
+    // with its kept metric part. Everything that evaluates right-hand sides through rhs()
+    // -- RK4 with a called plugin, and the FP64 right-hand side near the horizon -- runs
+    // in step_general, out of line: kept in the kernel, its calls' register needs made
+    // the C4 (Johannsen, Verlet) kernel 22 % slower on GB300 although it never ran them.
     static __device__ __forceinline__ bool step(Lane& L, const ImageConst& I, const RunConst& R) {
         float uf[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) uf[i] = ff_f(L.v[i]);
         const float h = adaptive_step_f32(R, I.mx, L.x[2], uf);
-        float du[4];
-        float dxc[4];  // O(h^2) part of the position increment
+        if (!(I.mx.r_fp64 > 0.f)) {
+            if (INTEG == FOORT_INTEGRATOR_VERLET) return step_verlet_cached(L, I, R, h, uf);
+            if (MixedMetric<MID>::kInline) return step_rk4_inline(L, I, R, h, uf);
+        }
+        const Incr d = step_general(I, R, L.x[1], L.x[2], L.v[1], L.v[2], F4{uf[0], uf[1], uf[2], uf[3]}, h);
+        L.rhs += d.rhs;
+        L.fp64 += d.fp64;
+        L.err |= d.err;
+        return advance(L, I, R, h, d.du, d.dxc);
+    }
+
+    // RK4 with the inlined plugin. The stage positions need only the velocities of earlier
+    // stages: x + h/2 u (stage 2) none, x + h/2 (u + h/2 k1) (stage 3) k1, x + h (u + h/2 k2)
+    // (stage 4) k2. So the metric part of stage 2 runs beside stage 1's, and those of stages
+    // 3 and 4 beside the contractions of stages 2 and 3: the dependent chain of a step is
+    // two metric evaluations and three contractions instead of four of each. Same
+    // operations, same results.
+    static __device__ __forceinline__ bool step_rk4_inline(Lane& L, const ImageConst& I, const RunConst& R, float h,
+                                                           const float uf[4]) {
+        float k1[4], k2[4], k3[4], k4[4], us[4], du[4], dxc[4];
+        const float hh = 0.5f * h;
+        const bool rlog = R.rlog != 0;
+        const MetricAt<float> m1 = metric_part<MID, float>(I.mx.q, I.mx, rlog, L.x[1], L.x[2]);
+        const MetricAt<float> m2 = metric_part<MID, float>(I.mx.q, I.mx, rlog, ff_add_f(L.x[1], hh * uf[1]),
+                                                           ff_add_f(L.x[2], hh * uf[2]));
+        accel_part(m1, rlog, uf, k1);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
+        const MetricAt<float> m3 = metric_part<MID, float>(I.mx.q, I.mx, rlog, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])),
+                                                           ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2])));
+        accel_part(m2, rlog, us, k2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
+        const MetricAt<float> m4 = metric_part<MID, float>(I.mx.q, I.mx, rlog, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])),
+                                                           ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])));
+        accel_part(m3, rlog, us, k3);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
+        accel_part(m4, rlog, us, k4);
+        rk4_combine(h, k1, k2, k3, k4, du, dxc);
+        L.rhs += 4;
+        return advance(L, I, R, h, du, dxc);
+    }
+
+    // The increments of one step taken by step_general, with its counts.
+    struct Incr {
+        float du[4], dxc[4];
+        uint32_t rhs, fp64, err;
+    };
+
+    // RK4 (Integrators.cpp:51-94) and velocity Verlet (Integrators.cpp:99-152) through
+    // rhs(), from the coordinates x1, theta and the velocity; in Verlet the velocity change
+    // of each iteration is formed as h/2 (a1_new - a1_old), free of cancellation.
+    static __device__ __noinline__ Incr step_general(const ImageConst& I, const RunConst& R, ff x1, ff th, ff v1, ff v2,
+                                                     F4 u4, float h) {
+        Incr d;
+        d.fp64 = 0;
+        d.err = 0;
+        const float uf[4] = {u4.x, u4.y, u4.z, u4.w};
         if (INTEG == FOORT_INTEGRATOR_RK4) {
             float k1[4], k2[4], k3[4], k4[4], us[4];
             const float hh = 0.5f * h;
-            if (MixedMetric<MID>::kInline && !(I.mx.r_fp64 > 0.f)) {
-                // The stage positions need only the velocities of earlier stages: x + h/2 u
-                // (stage 2) none, x + h/2 (u + h/2 k1) (stage 3) k1, x + h (u + h/2 k2)
-                // (stage 4) k2. So the metric part of stage 2 runs beside stage 1's, and
-                // those of stages 3 and 4 beside the contractions of stages 2 and 3: the
-                // dependent chain of a step is two metric evaluations and three
-                // contractions instead of four of each. Same operations, same results.
-                const bool rlog = R.rlog != 0;
-                const MetricAt<float> m1 = metric_part<MID, float>(I.mx.q, I.mx, rlog, L.x[1], L.x[2]);
-                const MetricAt<float> m2 = metric_part<MID, float>(I.mx.q, I.mx, rlog, ff_add_f(L.x[1], hh * uf[1]),
-                                                                   ff_add_f(L.x[2], hh * uf[2]));
-                accel_part(m1, rlog, uf, k1);
+            rhs(I, R, d.fp64, x1, th, uf, k1);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
-                const MetricAt<float> m3 = metric_part<MID, float>(
-                    I.mx.q, I.mx, rlog, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])),
-                    ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2])));
-                accel_part(m2, rlog, us, k2);
+            for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
+            rhs(I, R, d.fp64, ff_add_f(x1, hh * uf[1]), ff_add_f(th, hh * uf[2]), us, k2);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
-                const MetricAt<float> m4 = metric_part<MID, float>(
-                    I.mx.q, I.mx, rlog, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])),
-                    ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])));
-                accel_part(m3, rlog, us, k3);
+            for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
+            rhs(I, R, d.fp64, ff_add_f(x1, hh * (uf[1] + hh * k1[1])), ff_add_f(th, hh * (uf[2] + hh * k1[2])), us, k3);
 #pragma unroll
-                for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
-                accel_part(m4, rlog, us, k4);
-            } else {
-                rhs(I, R, L, L.x[1], L.x[2], uf, k1);
+            for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
+            rhs(I, R, d.fp64, ff_add_f(x1, h * (uf[1] + hh * k2[1])), ff_add_f(th, h * (uf[2] + hh * k2[2])), us, k4);
+            rk4_combine(h, k1, k2, k3, k4, d.du, d.dxc);
+            d.rhs = 4;
+            return d;
+        }
+        float a0[4], a1[4], vi[4];
+        rhs(I, R, d.fp64, x1, th, uf, a0);
+        const float hh2 = 0.5f * h * h;
 #pragma unroll
-                for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
-                rhs(I, R, L, ff_add_f(L.x[1], hh * uf[1]), ff_add_f(L.x[2], hh * uf[2]), us, k2);
+        for (int i = 0; i < 4; ++i) {
+            d.dxc[i] = hh2 * a0[i];
+            vi[i] = uf[i] + h * a0[i];
+        }
+        const ff x1n = ff_add_f(ff_add(x1, two_prod(h, v1.hi)), __fmaf_rn(h, v1.lo, d.dxc[1]));
+        const ff thn = ff_add_f(ff_add(th, two_prod(h, v2.hi)), __fmaf_rn(h, v2.lo, d.dxc[2]));
+        rhs(I, R, d.fp64, x1n, thn, vi, a1);
+        d.rhs = 2;
+        const float h2 = 0.5f * h;
 #pragma unroll
-                for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
-                rhs(I, R, L, ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])), ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2])),
-                    us, k3);
+        for (int i = 0; i < 4; ++i) d.du[i] = h2 * (a0[i] + a1[i]);
+        if (R.vtol > 0.0) {
+            const float tol2 = static_cast<float>(R.vtol * R.vtol);
+            float dv[4];  // first correction: nv - vi = h/2 (a1 - a0)
 #pragma unroll
-                for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
-                rhs(I, R, L, ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), ff_add_f(L.x[2], h * (uf[2] + hh * k2[2])),
-                    us, k4);
-            }
-            rk4_combine(h, k1, k2, k3, k4, du, dxc);
-            L.rhs += 4;
-        } else if (verlet_cached(I)) {
-            return step_verlet_cached(L, I, R, h, uf);
-        } else {
-            // velocity Verlet (Integrators.cpp:99-152); the velocity change of each
-            // iteration is formed as h/2 (a1_new - a1_old), free of cancellation.
-            float a0[4], a1[4], vi[4];
-            rhs(I, R, L, L.x[1], L.x[2], uf, a0);
-            const float hh2 = 0.5f * h * h;
+            for (int i = 0; i < 4; ++i) dv[i] = h2 * (a1[i] - a0[i]);
+            for (int it = 0;; ++it) {
+                float num = 0.f, den = 0.f;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                dxc[i] = hh2 * a0[i];
-                vi[i] = uf[i] + h * a0[i];
-            }
-            const ff x1n = ff_add_f(ff_add(L.x[1], two_prod(h, L.v[1].hi)), __fmaf_rn(h, L.v[1].lo, dxc[1]));
-            const ff thn = ff_add_f(ff_add(L.x[2], two_prod(h, L.v[2].hi)), __fmaf_rn(h, L.v[2].lo, dxc[2]));
-            rhs(I, R, L, x1n, thn, vi, a1);
-            L.rhs += 2;
-            const float h2 = 0.5f * h;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) du[i] = h2 * (a0[i] + a1[i]);
-            if (R.vtol > 0.0) {
-                const float tol2 = static_cast<float>(R.vtol * R.vtol);
-                // first correction: nv - vi = h/2 (a1 - a0)
-                float dv[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) dv[i] = h2 * (a1[i] - a0[i]);
-                for (int it = 0;; ++it) {
-                    float num = 0.f, den = 0.f;
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const float nvi = uf[i] + du[i];
-                        num += dv[i] * dv[i];
-                        den += nvi * nvi;
-                    }
-                    if (!(num > tol2 * den)) break;  // num / den > tol2 with den = |v|^2 > 0
-                    if (it >= R.verlet_cap) {
-                        L.err |= FOORT_ERR_VERLET_ITER;
-                        break;
-                    }
-                    float a1n[4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) vi[i] = uf[i] + du[i];
-                    rhs(I, R, L, x1n, thn, vi, a1n);
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        dv[i] = h2 * (a1n[i] - a1[i]);
-                        a1[i] = a1n[i];
-                        du[i] = h2 * (a0[i] + a1[i]);
-                    }
-                    L.rhs += 1;
+                for (int i = 0; i < 4; ++i) {
+                    const float nvi = uf[i] + d.du[i];
+                    num += dv[i] * dv[i];
+                    den += nvi * nvi;
                 }
+                if (!(num > tol2 * den)) break;  // num / den > tol2 with den = |v|^2 > 0
+                if (it >= R.verlet_cap) {
+                    d.err |= FOORT_ERR_VERLET_ITER;
+                    break;
+                }
+                float a1n[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) vi[i] = uf[i] + d.du[i];
+                rhs(I, R, d.fp64, x1n, thn, vi, a1n);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    dv[i] = h2 * (a1n[i] - a1[i]);
+                    a1[i] = a1n[i];
+                    d.du[i] = h2 * (a0[i] + a1[i]);
+                }
+                d.rhs += 1;
             }
         }
-        return advance(L, I, R, h, du, dxc);
+        return d;
     }
 
     // Velocity Verlet (Integrators.cpp:99-152) with one metric part per step. Every
@@ -480,7 +509,8 @@ struct MixedEngine {
         }
         const ff x1n = ff_add_f(ff_add(L.x[1], two_prod(h, L.v[1].hi)), __fmaf_rn(h, L.v[1].lo, dxc[1]));
         const ff thn = ff_add_f(ff_add(L.x[2], two_prod(h, L.v[2].hi)), __fmaf_rn(h, L.v[2].lo, dxc[2]));
-        const MetricAt<float> mn = metric(I, rlog, x1n, thn);
+        // inlined for every plugin: this is the step's only metric part
+        const MetricAt<float> mn = metric_part<MID, float>(I.mx.q, I.mx, rlog, x1n, thn);
         accel_part(mn, rlog, vi, a1);
         L.rhs += 2;
         const float h2 = 0.5f * h;
@@ -533,10 +563,13 @@ struct MixedEngine {
         // ulp without that bias: q1 = q0 + (h - 6 q0) / 6.
         const float q0 = __fmul_rn(h, 0.166666672f);
         const float h6 = __fmaf_rn(__fmaf_rn(-6.f, q0, h), 0.166666672f, q0), hh6 = __fmul_rn(h, h6);
+        // Each rounding is written out, so that the compiler cannot fuse the products that
+        // produced k4 (one-lane kernel) into these sums: the two-lane kernel, whose k
+        // arrive by shuffle, computes the same roundings.
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            du[i] = h6 * (k1[i] + 2.f * k2[i] + 2.f * k3[i] + k4[i]);
-            dxc[i] = hh6 * (k1[i] + k2[i] + k3[i]);
+            du[i] = __fmul_rn(h6, __fadd_rn(__fmaf_rn(2.f, k3[i], __fmaf_rn(2.f, k2[i], k1[i])), k4[i]));
+            dxc[i] = __fmul_rn(hh6, __fadd_rn(__fadd_rn(k1[i], k2[i]), k3[i]));
         }
     }
 
