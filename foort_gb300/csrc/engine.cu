@@ -637,7 +637,7 @@ const void* fp64_kernel(int metric_id, int integ) {
 // host, foort_noalloc_scratch names that array only as a symbol: its device address on
 // the current device comes from cudaGetSymbolAddress, looked up once per device.
 
-static_assert(sizeof(ImageConst) == 664, "FOORT_NOALLOC_SCRATCH_BYTES assumes 664-byte image constants");
+static_assert(sizeof(ImageConst) == 672, "FOORT_NOALLOC_SCRATCH_BYTES assumes 672-byte image constants");
 static_assert(kNumCtr * sizeof(unsigned long long) <= 256, "the counters take the first 256 bytes");
 
 static __device__ __align__(256) unsigned char foort_noalloc_scratch[FOORT_NOALLOC_SCRATCH_BYTES];

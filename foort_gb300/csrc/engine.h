@@ -30,6 +30,7 @@ struct MixedConst {
     float eqthr[2];    // EquatorialPasses threshold: pi / 2 * Threshold
     float eps[2];      // Integrators::epsilon
     float hmin;        // Integrators::SmallestPossibleStepsize
+    float vtol2;       // VerletVelocityTolerance squared (0: no velocity iterations)
 };
 
 // Per-image constants, computed once on the host (ViewScreen.cpp:10-73).

@@ -457,8 +457,8 @@ struct MixedEngine {
         const float h2 = 0.5f * h;
 #pragma unroll
         for (int i = 0; i < 4; ++i) d.du[i] = h2 * (a0[i] + a1[i]);
-        if (R.vtol > 0.0) {
-            const float tol2 = static_cast<float>(R.vtol * R.vtol);
+        if (I.mx.vtol2 > 0.f) {
+            const float tol2 = I.mx.vtol2;
             float dv[4];  // first correction: nv - vi = h/2 (a1 - a0)
 #pragma unroll
             for (int i = 0; i < 4; ++i) dv[i] = h2 * (a1[i] - a0[i]);
@@ -516,8 +516,8 @@ struct MixedEngine {
         const float h2 = 0.5f * h;
 #pragma unroll
         for (int i = 0; i < 4; ++i) du[i] = h2 * (a0[i] + a1[i]);
-        if (R.vtol > 0.0) {
-            const float tol2 = static_cast<float>(R.vtol * R.vtol);
+        if (I.mx.vtol2 > 0.f) {
+            const float tol2 = I.mx.vtol2;
             float dv[4];  // first correction: nv - vi = h/2 (a1 - a0)
 #pragma unroll
             for (int i = 0; i < 4; ++i) dv[i] = h2 * (a1[i] - a0[i]);

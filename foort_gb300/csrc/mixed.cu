@@ -1,4 +1,6 @@
 // Host side of the mixed-precision kernels: kernel registry and per-image constants.
+#include <algorithm>
+#include <cfloat>
 #include <cmath>
 
 #include "kernel_mixed.cuh"
@@ -63,6 +65,8 @@ void fill_mixed_constants(int metric_id, ImageConst& ic, const RunConst& rc) {
     ff_split(kRefPi / 2.0 * rc.eq_thr, mx.eqthr[0], mx.eqthr[1]);
     ff_split(rc.eps, mx.eps[0], mx.eps[1]);
     mx.hmin = static_cast<float>(rc.hmin);
+    // a positive tolerance whose square is below FP32's range still iterates (as with 0)
+    mx.vtol2 = rc.vtol > 0.0 ? std::max(static_cast<float>(rc.vtol * rc.vtol), FLT_MIN) : 0.f;
 }
 
 }  // namespace foort

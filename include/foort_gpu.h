@@ -236,7 +236,7 @@ int foort_gpu_integrate_async(foort_ctx* ctx, const foort_pixel* d_px, uint64_t 
  * There is no cancel flag; the step budget follows foort_gpu_integrate()'s default.
  * Errors are reported through foort_gpu_last_error(NULL). */
 #define FOORT_NOALLOC_MAX_IMAGES 256u
-#define FOORT_NOALLOC_SCRATCH_BYTES (256u + 664u * FOORT_NOALLOC_MAX_IMAGES) /* 170,240 */
+#define FOORT_NOALLOC_SCRATCH_BYTES (256u + 672u * FOORT_NOALLOC_MAX_IMAGES) /* 172,288 */
 int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foort_pixel* d_px, uint64_t n,
                                 foort_result* d_out, void* cuda_stream, foort_stats* stats);
 
