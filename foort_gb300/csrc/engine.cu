@@ -265,7 +265,7 @@ int ensure_capacity(foort_ctx* ctx, uint64_t n) {
 }
 
 int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, cudaStream_t st,
-           const unsigned long long* gp_plan = nullptr, double* gp_out = nullptr) {
+           GeoposRec* gp_plan = nullptr) {
     LaunchShape ls;
     int rc = choose_launch(ctx, ctx->rc, n, ctx->num_sms, ctx->block_size, ctx->blocks_per_sm, ctx->lanes, ls);
     if (rc) return rc;
@@ -283,7 +283,6 @@ int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_
     A.cancel = ctx->d_cancel;
     A.budget = ctx->budget;
     A.gp_plan = gp_plan;
-    A.gp_out = gp_out;
     if (!A.budget && !(ctx->rc.term_flags & FOORT_TERM_TIMEOUT)) {
         // Without TimeOut a geodesic may never terminate (the reference would loop
         // forever); a finite default budget keeps every launch finite.
@@ -456,14 +455,14 @@ int foort_gpu_positions(foort_ctx* ctx, const foort_pixel* px, uint64_t n, const
     if (n && (!px || !first || !counts)) return fail(ctx, FOORT_E_BADARG, "NULL pixel, result or count buffer");
     if (!(ctx->desc.diag_flags & FOORT_DIAG_GEODESIC_POSITION))
         return fail(ctx, FOORT_E_BADARG, "the GeodesicPosition diagnostic is not turned on");
-    std::vector<unsigned long long> plan(3 * n);
+    std::vector<GeoposRec> plan(n);
+    std::vector<uint64_t> first_slot(n);
     uint64_t total = 0;
     for (uint64_t i = 0; i < n; ++i) {
         uint64_t M, j, kept;
         geopos_plan(ctx->desc, first[i].steps, first[i].term, M, j, kept);
-        plan[3 * i] = total;
-        plan[3 * i + 1] = j;
-        plan[3 * i + 2] = M;
+        first_slot[i] = total;
+        plan[i] = GeoposRec{nullptr, j, M, 0, 0};
         counts[i] = kept;
         total += kept;
     }
@@ -475,17 +474,18 @@ int foort_gpu_positions(foort_ctx* ctx, const foort_pixel* px, uint64_t n, const
     int rc = finish(ctx);
     if (rc != FOORT_OK && rc != FOORT_E_BUDGET && rc != FOORT_E_CANCELLED) return rc;
     if ((rc = ensure_capacity(ctx, n))) return rc;
-    unsigned long long* d_plan = nullptr;
+    GeoposRec* d_plan = nullptr;
     double* d_pts = nullptr;
     std::vector<foort_result> again(n);
     auto body = [&]() -> int {
         cudaStream_t st = ctx->stream;
-        CK(cudaMalloc(&d_plan, plan.size() * sizeof(unsigned long long)));
+        CK(cudaMalloc(&d_plan, plan.size() * sizeof(GeoposRec)));
         CK(cudaMalloc(&d_pts, std::max<uint64_t>(1, total) * 4 * sizeof(double)));
         CK(cudaMemsetAsync(d_pts, 0xFF, std::max<uint64_t>(1, total) * 4 * sizeof(double), st));  // NaN
+        for (uint64_t i = 0; i < n; ++i) plan[i].dst = d_pts + 4 * first_slot[i];  // device addresses
         CK(cudaMemcpyAsync(ctx->d_px, px, n * sizeof(foort_pixel), cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(d_plan, plan.data(), plan.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, st));
-        int r = launch(ctx, ctx->d_px, n, ctx->d_out, st, d_plan, d_pts);
+        CK(cudaMemcpyAsync(d_plan, plan.data(), plan.size() * sizeof(GeoposRec), cudaMemcpyHostToDevice, st));
+        int r = launch(ctx, ctx->d_px, n, ctx->d_out, st, d_plan);
         if (r) return r;
         CK(cudaMemcpyAsync(points, d_pts, total * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(again.data(), ctx->d_out, n * sizeof(foort_result), cudaMemcpyDeviceToHost, st));
@@ -497,7 +497,7 @@ int foort_gpu_positions(foort_ctx* ctx, const foort_pixel* px, uint64_t n, const
     if (rc != FOORT_OK) return rc;
     // the second pass must retrace the first: same steps for every recorded geodesic
     for (uint64_t i = 0; i < n; ++i)
-        if (plan[3 * i + 2] && again[i].steps != first[i].steps)
+        if (plan[i].M && again[i].steps != first[i].steps)
             return fail(ctx, FOORT_E_NUMERIC, "geodesic " + std::to_string(i) + " took " +
                                                   std::to_string(again[i].steps) + " steps on the second pass, " +
                                                   std::to_string(first[i].steps) + " on the first");

@@ -90,7 +90,7 @@ struct Fp64Engine {
         uint32_t rhs = 0;
         uint32_t fp64 = 0;
         int32_t term = 0;
-        GeoposRec gp;  // set by the loop before init
+        GeoposRec gp;  // set by the loop before init (dst null: not recording)
         FdParts P;     // Verlet: the parts at x (computed at the previous step's new position)
     };
 

@@ -192,7 +192,7 @@ struct MixedEngine {
         TermState T;
         // diagnostics on the compensated state
         int32_t quad, passes;
-        uint64_t cE, cC;
+        StepCount cE, cC;
         ff prev;      // previous theta sample (hi = -1: none yet)
         ff rmin;      // closest radius so far; ln r in log-r mode
         bool has_rmin;
@@ -201,7 +201,7 @@ struct MixedEngine {
         uint32_t rhs = 0;
         uint32_t fp64 = 0;
         int32_t term = 0;
-        GeoposRec gp;  // set by the loop before init
+        GeoposRec gp;  // set by the loop before init (dst null: not recording)
         MetricAt<float> mc;  // Verlet: the metric part at the current (x1, theta)
     };
 
