@@ -11,6 +11,7 @@
 import ctypes as C
 import os
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -66,3 +67,18 @@ def test_fp32_acceleration_accuracy(tmp_path):
         if name == "ff_sincos":
             # the mixed kernel's sin/cos: a few roundings, relative, also next to the poles
             assert mx < 5e-7, line
+
+
+def test_generated_plugins_match_the_generator(tmp_path):
+    """gen_christoffel.inc is what foort_gb300/gen/gen_christoffel.py prints: the
+    generator's own checks (Rasheed-Larsen's H3 divides the numerators it removes; the
+    quotient has the coefficients the constants code assumes) pass, and the file is
+    up to date."""
+    pytest.importorskip("sympy")
+    out = tmp_path / "gen.inc"
+    with open(out, "w") as f:
+        subprocess.run([sys.executable, os.path.join(ROOT, "foort_gb300", "gen", "gen_christoffel.py")], check=True,
+                       stdout=f, cwd=os.path.join(ROOT, "foort_gb300", "gen"), timeout=600)
+    with open(os.path.join(ROOT, "foort_gb300", "csrc", "gen_christoffel.inc")) as f:
+        committed = f.read()
+    assert out.read_text() == committed
