@@ -14,7 +14,9 @@ import pytest
 from conftest import GOLDEN
 from foort_gb300 import abi
 
-REF_CFG = os.path.join("/root/reference", "FOORT")
+import oracle  # noqa: E402  (only for the location of the reference's sources)
+
+REF_CFG = oracle.REF_SRC
 
 
 def load(text):
