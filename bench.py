@@ -227,6 +227,7 @@ def run_reference(args, rank):
     else:
         side = int((math.sqrt(spec["initial_pixels"]) - 1) * 2 ** (spec["max_subdivide"] - 1) + 1)
     grid = reference_run_pixels(args)
+    run_px = grid is not None  # the pixel set of the reference's complete C2 run (5 rounds)
     where = f"of the reference's own complete run ({len(grid)} pixels of the {side}^2 grid)" if grid is not None \
         else f"of the {side}^2 grid"
     if grid is None:
@@ -247,7 +248,8 @@ def run_reference(args, rank):
         "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(r[2] for r in rates) / len(rates),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_block(wl, args, side=side),
+        "config": config_block(wl, args, side=side, rounds=5 if run_px else None,
+                               geod=len(grid) if run_px else None),
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": nthreads, "kind": kind_name,
                          "sample": f"{rates[-1][1]} seeded-random pixels {where} per step; "
                                    + ("the reference compiled from its sources with its own -Ofast -fopenmp flags"
