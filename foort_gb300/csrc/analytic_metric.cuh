@@ -100,6 +100,195 @@ FOORT_DEFINE_MIXED_METRIC(kJohannsen, FOORT_MIXED_BODY_JOHANNSEN, false)
 FOORT_DEFINE_MIXED_METRIC(kFlat, FOORT_MIXED_BODY_FLAT, true)
 FOORT_DEFINE_MIXED_METRIC(kRasheedLarsen, FOORT_MIXED_BODY_RASHEEDLARSEN, false)
 
+// ---- Manko-Novikov, by forward-mode differentiation ---------------------------------
+// Its metric functions are exponentials of sums of Legendre terms over powers of
+// R = sqrt(x^2 + y^2 - 1) (Metric.cpp:511-566); sympy's expanded derivatives of them
+// would be enormous. Instead the metric is evaluated once on dual numbers carrying the
+// value and its derivatives in r and theta, which gives d_r g and d_theta g exactly up to
+// rounding. Restated for the same values with these cancellation-free forms (x - 1 =
+// (r - r_+)/k, so near the horizon nothing is formed as a difference of near-equal
+// numbers):
+//   x^2 - 1 = dp (x + 1) / k,  1 - y^2 = sin^2,  R^2 = (x^2 - 1) + y^2,
+//   x^2 - y^2 = (x^2 - 1) + sin^2,  Delta = dp dm,  rho^2 = Delta + k^2 sin^2,
+// and the inverse of the (t, phi) block from its determinant, exactly -Delta sin^2:
+//   g^tt = -g_phiphi / (Delta sin^2), g^tphi = g_tphi / (Delta sin^2),
+//   g^phiphi = -g_tt / (Delta sin^2).
+template <typename T>
+struct D2 {
+    T v, r, h;  // value, d/dr, d/dtheta
+};
+template <typename T>
+FOORT_HD D2<T> operator+(D2<T> a, D2<T> b) { return {a.v + b.v, a.r + b.r, a.h + b.h}; }
+template <typename T>
+FOORT_HD D2<T> operator-(D2<T> a, D2<T> b) { return {a.v - b.v, a.r - b.r, a.h - b.h}; }
+template <typename T>
+FOORT_HD D2<T> operator-(D2<T> a) { return {-a.v, -a.r, -a.h}; }
+template <typename T>
+FOORT_HD D2<T> operator*(D2<T> a, D2<T> b) { return {a.v * b.v, a.r * b.v + a.v * b.r, a.h * b.v + a.v * b.h}; }
+template <typename T>
+FOORT_HD D2<T> operator*(T c, D2<T> a) { return {c * a.v, c * a.r, c * a.h}; }
+template <typename T>
+FOORT_HD D2<T> operator+(T c, D2<T> a) { return {c + a.v, a.r, a.h}; }
+template <typename T>
+FOORT_HD D2<T> inv(D2<T> a) {  // 1 / a
+    const T i = rcp(a.v), i2 = -i * i;
+    return {i, i2 * a.r, i2 * a.h};
+}
+template <typename T>
+FOORT_HD D2<T> d_sqrt(D2<T> a) {
+    const T s = ::sqrt(a.v), d = T(0.5) * rcp(s);
+    return {s, d * a.r, d * a.h};
+}
+template <typename T>
+FOORT_HD D2<T> d_exp(D2<T> a) {
+    const T e = ::exp(a.v);
+    return {e, e * a.r, e * a.h};
+}
+
+template <typename T>
+FOORT_HD D2<T> d_cast(D2<double> a) {
+    return {T(a.v), T(a.r), T(a.h)};
+}
+
+// q: a, alpha3, alpha, k (make_metric_const). rd, dpd = r - r_+ (r_+ = 1 + k), sd, cd:
+// the position in FP64; dp, dm, s, c: the same in T.
+// The exponents' arguments are computed in FP64 from the FP64 position, whatever T is:
+// - 1 - (x - y) S1 and -1 + (x + y) S2 are sums of O(1) terms whose leading orders cancel
+//   through 1/x^2, so in FP32 arithmetic their absolute error stays ~6e-8 while the
+//   values fall off like 1/x^3; an exponent's absolute error becomes the metric's
+//   relative error (2e-6 at alpha3 = 13, the reference's Test.cfg value);
+// - the exponents are sensitive to the position (factors of 2 alpha3): r and theta
+//   rounded to FP32 put p99 7e-6 on the FP32 acceleration at alpha3 = 13, FP64 inputs
+//   with only the exponentials rounded to FP32 2e-7 (measured on the CPU).
+// ~250 FP64 operations per evaluation. The rest is in T.
+template <typename T>
+FOORT_HD void mn_eval(const T* q, double rd, double dpd, double sd, double cd, T dp, T dm, T s, T c, G5T<T>& dr,
+                      G5T<T>& dh, G5T<T>& gu, T& grr) {
+    // -- the exponents' arguments (FP64)
+    const double a3d = q[1], kd = q[3], ikd = 1.0 / kd;
+    const D2<double> X = {(rd - 1.0) * ikd, ikd, 0.0};
+    const D2<double> Y = {cd, 0.0, -sd};
+    const D2<double> XM1 = ikd * D2<double>{dpd, 1.0, 0.0};  // x - 1
+    const D2<double> X2M1 = XM1 * (2.0 + XM1);                // x^2 - 1
+    const D2<double> iR = inv(d_sqrt(X2M1 + Y * Y));
+    const D2<double> t = X * Y * iR;  // the Legendre argument xy / R
+    const D2<double> t2 = t * t;
+    const D2<double> P1 = t;
+    const D2<double> P2 = 0.5 * (3.0 * t2 + D2<double>{-1.0, 0.0, 0.0});
+    const D2<double> P3 = 0.5 * t * (5.0 * t2 + D2<double>{-3.0, 0.0, 0.0});
+    const D2<double> P4 = 0.125 * (35.0 * t2 * t2 - 30.0 * t2 + D2<double>{3.0, 0.0, 0.0});
+    const D2<double> S1 = iR * (1.0 + iR * (P1 + iR * (P2 + iR * P3)));   // 1/R + P1/R^2 + P2/R^3 + P3/R^4
+    const D2<double> S2 = iR * (1.0 + iR * (-P1 + iR * (P2 - iR * P3)));  // 1/R - P1/R^2 + P2/R^3 - P3/R^4
+    const D2<double> iR4 = (iR * iR) * (iR * iR);
+    const D2<double> Ea = (2.0 * a3d) * (1.0 + -((X - Y) * S1));
+    const D2<double> Eb = (2.0 * a3d) * (-1.0 + (X + Y) * S2);
+    const D2<double> psi2 = (2.0 * a3d) * (P3 * iR4);  // 2 psi
+    const D2<double> gp2 = (4.0 * a3d * a3d) * ((P4 * P4 - P3 * P3) * (iR4 * iR4)) +
+                           (4.0 * a3d) * ((-Y + iR * (X * P1 + iR * (-(Y * P2) + iR * (X * P3)))) * iR);  // 2 gamma'
+    // -- the metric (T), without the reference's 1/AA: AA vanishes where g_tt does, and
+    // omega and g_phiphi divide by it with terms that cancel there. With E = e^(2 psi),
+    // G = e^(2 gamma'), c0 = 4 k alpha / (1 - alpha^2) and the identity
+    //   4 CC^2 - (x^2 - 1)(1 - y^2) BB^2 = AA Q,
+    //   Q = -s^2 (x-1)^4 a^2 b^2 + (x^2-1)(1+y)^4 a^2 - 2 s^2 (x^2-1)(x^2-y^2) a b
+    //       + (x^2-1)(1-y)^4 b^2 - s^2 (x+1)^4     (a = aa, b = bb, s^2 = 1 - y^2),
+    // the components are g_tt = -E AA/BB, g_tphi = (2k CC - c0 E AA)/BB,
+    // g_phiphi = (-k^2 Q/E + 4k c0 CC - c0^2 E AA)/BB, g_thth = G rho^2 BB / (E (x^2 - y^2)
+    // (1 - alpha^2)^2), g_rr = g_thth / Delta: the reference's expressions rearranged.
+    const T al = q[2], k = q[3];
+    const D2<T> y = d_cast<T>(Y);
+    const D2<T> xm1 = d_cast<T>(XM1);
+    const D2<T> xp1 = T(2) + xm1, x = T(1) + xm1;
+    const D2<T> x2m1 = d_cast<T>(X2M1);
+    const D2<T> s2 = {s * s, T(0), T(2) * s * c};
+    const D2<T> aa = (-al) * d_exp(d_cast<T>(Ea));
+    const D2<T> bb = al * d_exp(d_cast<T>(Eb));
+    const D2<T> ab = aa * bb;
+    const D2<T> ab1 = T(1) + ab;
+    const D2<T> bma = bb - aa;
+    const D2<T> AA = x2m1 * ab1 * ab1 - s2 * bma * bma;
+    const D2<T> b1 = xp1 + xm1 * ab;
+    const D2<T> yp1 = T(1) + y, ym1 = T(1) + -y;  // 1 + y, 1 - y
+    const D2<T> b2 = yp1 * aa + ym1 * bb;
+    const D2<T> BB = b1 * b1 + b2 * b2;
+    const D2<T> CC = x2m1 * ab1 * (bma - y * (aa + bb)) + s2 * bma * (ab1 + x * (T(1) + -ab));
+    const D2<T> xm1_2 = xm1 * xm1, xp1_2 = xp1 * xp1, yp1_2 = yp1 * yp1, ym1_2 = ym1 * ym1;
+    const D2<T> x2my2 = x2m1 + s2;  // x^2 - y^2
+    const D2<T> Q = -(s2 * (xm1_2 * xm1_2) * ab * ab) + x2m1 * (yp1_2 * yp1_2) * aa * aa -
+                    T(2) * (s2 * x2m1 * x2my2 * ab) + x2m1 * (ym1_2 * ym1_2) * bb * bb - s2 * (xp1_2 * xp1_2);
+    const T om2 = T(1) - al * al, c0 = T(4) * k * al * rcp(om2);
+    const D2<T> E = d_exp(d_cast<T>(psi2)), Ei = d_exp(d_cast<T>(-psi2));
+    const D2<T> iBB = inv(BB);
+    const D2<T> EAA = E * AA;
+    const D2<T> del = {dp * dm, dp + dm, T(0)};
+    const D2<T> rho2 = del + (k * k) * s2;
+    const D2<T> g_tt = -(EAA * iBB);
+    const D2<T> g_tp = ((T(2) * k) * CC - c0 * EAA) * iBB;
+    const D2<T> g_pp = ((-(k * k)) * (Q * Ei) + (T(4) * k * c0) * CC - (c0 * c0) * EAA) * iBB;
+    const D2<T> g_hh = d_exp(d_cast<T>(gp2)) * rho2 * BB * Ei * inv((om2 * om2) * x2my2);
+    const D2<T> g_rr = g_hh * inv(del);
+    dr = {g_tt.r, g_tp.r, g_rr.r, g_hh.r, g_pp.r};
+    dh = {g_tt.h, g_tp.h, g_rr.h, g_hh.h, g_pp.h};
+    const T idet = rcp(del.v * s2.v);  // the (t, phi) block's determinant is -Delta sin^2
+    gu = {-g_pp.v * idet, g_tp.v * idet, rcp(g_rr.v), rcp(g_hh.v), -g_tt.v * idet};
+    grr = g_rr.v;
+}
+
+// The largest of |2 alpha3 (1 - (x - y) S1)|, |2 alpha3 (-1 + (x + y) S2)|, |2 psi| and
+// |2 gamma'| (the arguments of Manko-Novikov's exponentials, mn_eval) over theta at
+// radius r, in FP64 (host). FP32 carries an exponent with absolute error ~6e-8 times its
+// size, which becomes the relative error of the metric; near the horizon the exponents
+// grow without bound and the metric leaves FP32's range.
+inline double mn_max_exponent(const MetricConst& M, double r) {
+    const double a3 = M.q[1], k = M.q[3];
+    double worst = 0.0;
+    for (int i = 1; i < 360; ++i) {
+        const double th = 3.14159265358979323846 * i / 360.0, y = std::cos(th), s = std::sin(th);
+        const double x = (r - 1.0) / k, x2m1 = (x - 1.0) * (x + 1.0);
+        const double R = std::sqrt(x2m1 + y * y), iR = 1.0 / R, t = x * y * iR, t2 = t * t;
+        const double P1 = t, P2 = 0.5 * (3 * t2 - 1), P3 = 0.5 * t * (5 * t2 - 3), P4 = 0.125 * (35 * t2 * t2 - 30 * t2 + 3);
+        const double S1 = iR * (1 + iR * (P1 + iR * (P2 + iR * P3))), S2 = iR * (1 + iR * (-P1 + iR * (P2 - iR * P3)));
+        const double iR4 = iR * iR * iR * iR;
+        const double ea = 2 * a3 * (1 - (x - y) * S1), eb = 2 * a3 * (-1 + (x + y) * S2);
+        const double psi = a3 * P3 * iR4;
+        const double gp = 2 * a3 * a3 * (P4 * P4 - P3 * P3) * iR4 * iR4 +
+                          2 * a3 * (-y + iR * (x * P1 + iR * (-y * P2 + iR * x * P3))) * iR;
+        (void)s;
+        const double m = std::fmax(std::fmax(std::fabs(ea), std::fabs(eb)), std::fmax(std::fabs(2 * psi), std::fabs(2 * gp)));
+        if (!(m <= worst)) worst = m;  // a NaN counts as unbounded
+    }
+    return worst;
+}
+
+// The radius inside which Manko-Novikov's mixed-precision right-hand side is taken in
+// FP64: scanning inward from r = 10^4, the first radius at which an exponent exceeds
+// max_exponent, with r - r_+ times 1.1 (everything inside it uses FP64).
+constexpr double kMnMaxFp32Exponent = 8.0;
+inline double mn_fp64_radius(const MetricConst& M, double max_exponent) {
+    const double rp = 1.0 + M.q[3];
+    for (double r = 1e4; r > rp; r = rp + (r - rp) * 0.97)
+        if (!(mn_max_exponent(M, r) <= max_exponent)) return rp + (r - rp) * 1.1;
+    return rp;
+}
+
+template <>
+struct MixedMetric<kMankoNovikov> {
+    static constexpr bool kAvailable = true;
+    static constexpr bool kInline = false;
+    // from the position in T only (FP64 callers)
+    template <typename T>
+    static FOORT_HD void eval(const T* q, T r, T dp, T dm, T s, T c, G5T<T>& dr, G5T<T>& dh, G5T<T>& gu, T& grr) {
+        (void)r;
+        mn_eval<T>(q, double(r), double(dp), double(s), double(c), dp, dm, s, c, dr, dh, gu, grr);
+    }
+    // with the position also in FP64 (the mixed kernel has it in float-float)
+    template <typename T>
+    static FOORT_HD void eval_hi(const T* q, double rd, double dpd, double sd, double cd, T dp, T dm, T s, T c,
+                                 G5T<T>& dr, G5T<T>& dh, G5T<T>& gu, T& grr) {
+        (void)rd;
+        mn_eval<T>(q, rd, dpd, sd, cd, dp, dm, s, c, dr, dh, gu, grr);
+    }
+};
+
 // The plugins' constants q[]: the metric constants of make_metric_const for Kerr,
 // Johannsen and flat space; for Rasheed-Larsen the slots of its rewritten form
 // (gen_christoffel.py), from its rescaled m, a, p, q.
@@ -114,7 +303,8 @@ inline void mixed_metric_constants(int id, const MetricConst& M, double out[kMix
 }
 
 // r_+ and r_- of the plugin's Delta = (r - r_+)(r - r_-) = r^2 - 2 m r + a^2: m = 1 for
-// Kerr and Johannsen, Rasheed-Larsen's rescaled m; none for flat space.
+// Kerr and Johannsen, Rasheed-Larsen's rescaled m; 1 -+ k for Manko-Novikov; none for
+// flat space.
 inline void mixed_horizons(int id, const MetricConst& M, double& rp, double& rm) {
     rp = rm = 0.0;
     if (id == kKerr || id == kJohannsen) {
@@ -125,6 +315,9 @@ inline void mixed_horizons(int id, const MetricConst& M, double& rp, double& rm)
         const double a = M.q[0], m = M.q[1];
         rp = m + std::sqrt(m * m - a * a);
         rm = m - std::sqrt(m * m - a * a);
+    } else if (id == kMankoNovikov) {  // Delta = (r - 1)^2 - k^2
+        rp = 1.0 + M.q[3];
+        rm = 1.0 - M.q[3];
     }
 }
 

@@ -111,7 +111,16 @@ __device__ __forceinline__ MetricAt<T> metric_part(const T* q, const MixedConst&
     }
     MetricAt<T> m;
     T grr;
-    MixedMetric<MID>::template eval<T>(q, r, dp, dm, s, c, m.d1, m.d2, m.gu, grr);
+    if constexpr (MID == kMankoNovikov && sizeof(T) == sizeof(float)) {
+        // the plugin's FP64 block (its exponents) takes the position in FP64
+        const double x1d = double(x1.hi) + double(x1.lo);
+        const double rd = rlog ? exp(x1d) : x1d;
+        double sd, cd;
+        sincos(double(th.hi) + double(th.lo), &sd, &cd);
+        MixedMetric<MID>::template eval_hi<T>(q, rd, rd - mc.rpv, sd, cd, dp, dm, s, c, m.d1, m.d2, m.gu, grr);
+    } else {
+        MixedMetric<MID>::template eval<T>(q, r, dp, dm, s, c, m.d1, m.d2, m.gu, grr);
+    }
     if (rlog) scale_log_r(r, m.d1, m.d2, m.gu);
     return m;
 }

@@ -49,6 +49,7 @@ extern "C" int foort_metric_christoffel(int32_t metric_id, const double* params,
     case FOORT_METRIC_JOHANNSEN: return christoffel_host<kJohannsen>(params, rlog != 0, x, gamma);
     case FOORT_METRIC_FLAT: return christoffel_host<kFlat>(params, false, x, gamma);
     case FOORT_METRIC_RASHEED_LARSEN: return christoffel_host<kRasheedLarsen>(params, rlog != 0, x, gamma);
+    case FOORT_METRIC_MANKO_NOVIKOV: return christoffel_host<kMankoNovikov>(params, rlog != 0, x, gamma);
     default: return FOORT_E_UNSUPPORTED;
     }
 }

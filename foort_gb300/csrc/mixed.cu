@@ -12,15 +12,17 @@ const void* mixed_kernel_kerr(int integrator, bool decide64);
 const void* mixed_kernel_joh(int integrator, bool decide64);
 const void* mixed_kernel_flat(int integrator, bool decide64);
 const void* mixed_kernel_rl(int integrator, bool decide64);
+const void* mixed_kernel_mn(int integrator, bool decide64);
 
-// Mixed kernels exist for the metrics with analytic derivatives (gen_christoffel.py);
-// Manko-Novikov runs in FP64 only.
+// Mixed kernels for every metric: analytic derivatives generated by gen_christoffel.py,
+// and for Manko-Novikov by forward-mode differentiation (analytic_metric.cuh).
 const void* mixed_kernel_variant(int metric_id, int integ, bool decide64) {
     switch (metric_id) {
     case kKerr: return mixed_kernel_kerr(integ, decide64);
     case kJohannsen: return mixed_kernel_joh(integ, decide64);
     case kFlat: return mixed_kernel_flat(integ, decide64);
     case kRasheedLarsen: return mixed_kernel_rl(integ, decide64);
+    case kMankoNovikov: return mixed_kernel_mn(integ, decide64);
     default: return nullptr;
     }
 }
@@ -54,7 +56,12 @@ void fill_mixed_constants(int metric_id, ImageConst& ic, const RunConst& rc) {
     ff_split(rm > 0 ? std::log(rm) : 0.0, mx.lrm[0], mx.lrm[1]);
     const bool rlog = rc.rlog != 0;
     auto coord = [rlog](double r) { return rlog ? std::log(r) : r; };
-    mx.r_fp64 = (rc.mixed_fp64_margin > 0.0 && rp > 0.0) ? static_cast<float>(coord(rp + rc.mixed_fp64_margin)) : 0.f;
+    double r_fp64 = (rc.mixed_fp64_margin > 0.0 && rp > 0.0) ? rp + rc.mixed_fp64_margin : 0.0;
+    // Manko-Novikov's exponents grow without bound toward the horizon and its metric
+    // leaves FP32's range there: inside the radius where one exceeds 8 (e^8 ~ 3e3), the
+    // right-hand side is always taken in FP64
+    if (metric_id == kMankoNovikov) r_fp64 = std::max(r_fp64, mn_fp64_radius(ic.m, kMnMaxFp32Exponent));
+    mx.r_fp64 = r_fp64 > 0.0 ? static_cast<float>(coord(r_fp64)) : 0.f;
     const double rh = ic.m.rh;
     ff_split(coord(rh * (1 + ic.h_eps)), mx.hthr[0], mx.hthr[1]);
     ff_split(ic.h_eps > 0 ? coord(ic.h_eps) : (rlog ? -HUGE_VAL : 0.0), mx.hthr0[0], mx.hthr0[1]);

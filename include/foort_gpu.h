@@ -303,7 +303,7 @@ int foort_gpu_has_kernel(int32_t metric_id, int32_t integrator_id, int32_t preci
  * coordinates: x[1] = ln r when rlog) from the analytic metric derivatives the
  * mixed-precision kernel uses, evaluated in FP64 on the host. Replaces
  * Metric::getChristoffel_udd (Metric.cpp:14-55), which differentiates numerically.
- * FOORT_E_UNSUPPORTED for metrics without an analytic plugin (Manko-Novikov). */
+ * FOORT_E_UNSUPPORTED for an unknown metric_id. */
 int foort_metric_christoffel(int32_t metric_id, const double* metric_params, int32_t rlog, const double* x,
                              double* gamma);
 

@@ -18,7 +18,7 @@
 using namespace foort;
 
 template <int MID>
-void run(const char* name, const double* params, bool rlog) {
+void run(const char* name, const double* params, bool rlog, double r_from = 0.0) {
     MetricConst M = make_metric_const(MID, params);
     double qd[kMixedQ], rp, rm;
     mixed_metric_constants(MID, M, qd);
@@ -28,7 +28,7 @@ void run(const char* name, const double* params, bool rlog) {
     std::mt19937_64 rng(7);
     std::uniform_real_distribution<double> U(0.0, 1.0);
     std::vector<double> errs;
-    const double rlo = (rp > 0 ? rp : 1.0) + 0.01;
+    const double rlo = r_from > 0.0 ? r_from : (rp > 0 ? rp : 1.0) + 0.01;
     for (int k = 0; k < 20000; ++k) {
         const double r = rlo * std::pow(1000.0 / rlo, U(rng));
         const double th = 0.05 + (M_PI - 0.1) * U(rng);
@@ -57,7 +57,11 @@ void run(const char* name, const double* params, bool rlog) {
         ff_sincos(th_hi, static_cast<float>(th - th_hi), sf, cf);
         G5T<float> fr, fh, fu;
         float frr;
-        MixedMetric<MID>::template eval<float>(qf, rf, dpf, dmf, sf, cf, fr, fh, fu, frr);
+        if constexpr (MID == kMankoNovikov) {  // as the kernel calls it: the position also in FP64
+            MixedMetric<MID>::template eval_hi<float>(qf, r, r - rp, s, c, dpf, dmf, sf, cf, fr, fh, fu, frr);
+        } else {
+            MixedMetric<MID>::template eval<float>(qf, rf, dpf, dmf, sf, cf, fr, fh, fu, frr);
+        }
         float uf[4] = {static_cast<float>(u[0]), static_cast<float>(u[1]), static_cast<float>(u[2]), static_cast<float>(u[3])};
         float af[4];
         if (rlog) {
@@ -132,5 +136,14 @@ int main() {
     run<kRasheedLarsen>("rasheed_larsen_lorenzo_logr", rl_lorenzo, true);
     run<kRasheedLarsen>("rasheed_larsen_m1", rl_m1, false);
     run<kRasheedLarsen>("rasheed_larsen_default", rl_default, false);
+    // Manko-Novikov (a, alpha3): the reference's Test.cfg value alpha3 = 13, its default 5,
+    // and a mild 1; outside the radius inside which the kernel takes FP64
+    const double mn_sets[3][6] = {{0.94, 13.0}, {0.9, 5.0}, {0.7, 1.0}};
+    const char* mn_names[3] = {"manko_novikov_a0.94_alpha3_13", "manko_novikov_a0.9_alpha3_5",
+                               "manko_novikov_a0.7_alpha3_1"};
+    for (int i = 0; i < 3; ++i) {
+        const MetricConst M = make_metric_const(kMankoNovikov, mn_sets[i]);
+        run<kMankoNovikov>(mn_names[i], mn_sets[i], false, mn_fp64_radius(M, kMnMaxFp32Exponent));
+    }
     return 0;
 }

@@ -82,13 +82,12 @@ def test_create_rejects_bad_descriptors_without_touching_the_gpu(engine_lib):
 
 
 def test_kernel_registry(engine_lib):
-    """Every metric has FP64 kernels for both integrators; the mixed precision has them
-    for the metrics with analytic plugins (all but Manko-Novikov). Host-only query."""
+    """Every metric has FP64 and mixed-precision kernels for both integrators. Host-only
+    query."""
     for metric in (abi.METRIC_KERR, abi.METRIC_FLAT, abi.METRIC_RASHEED_LARSEN, abi.METRIC_JOHANNSEN,
                    abi.METRIC_MANKO_NOVIKOV):
         for integ in (abi.INTEGRATOR_RK4, abi.INTEGRATOR_VERLET):
             assert engine_lib.foort_gpu_has_kernel(metric, integ, abi.PREC_FP64) == 1
-            want = 0 if metric == abi.METRIC_MANKO_NOVIKOV else 1
-            assert engine_lib.foort_gpu_has_kernel(metric, integ, abi.PREC_MIXED) == want, (metric, integ)
+            assert engine_lib.foort_gpu_has_kernel(metric, integ, abi.PREC_MIXED) == 1, (metric, integ)
     assert engine_lib.foort_gpu_has_kernel(5, abi.INTEGRATOR_RK4, abi.PREC_FP64) == 0
     assert engine_lib.foort_gpu_has_kernel(abi.METRIC_KERR, 2, abi.PREC_FP64) == 0

@@ -25,7 +25,7 @@ RL_M1 = (0.0000292676523070559347272298622578, 0.0000292676523070559347272298622
          3.15470053516341633378322799917, 0.84529946483658456162619604143)
 CASES = [(0, (0.99,), 0), (0, (0.7,), 1), (3, (0.9, -0.6, 0, 0, 0), 0), (3, (0.7, 2.0, 0, 0, 0), 1),
          (3, (0.8, 1.0, 0.5, 0.2, 0.1), 0), (1, (), 0), (2, RL_LORENZO, 0), (2, RL_LORENZO, 1), (2, RL_M1, 0),
-         (2, (1.0, 0.5, 2.0, 2.0), 0)]
+         (2, (1.0, 0.5, 2.0, 2.0), 0), (4, (0.94, 13.0), 0), (4, (0.9, 5.0), 1), (4, (0.7, 1.0), 0)]
 
 
 @pytest.mark.parametrize("metric,params,rlog", CASES)
@@ -43,14 +43,17 @@ def test_analytic_christoffel_equals_finite_differences(engine_lib, oracle_mod, 
         assert engine_lib.foort_metric_christoffel(metric, p.ctypes.data, rlog, x.ctypes.data, ga.ctypes.data) == 0
         ol.oracle_christoffel(metric, p.ctypes.data, rlog, 1e-5, x.ctypes.data, gb.ctypes.data)
         worst = max(worst, np.abs(ga - gb).max() / np.abs(gb).max())
-    assert worst < 1e-7, worst
+    # Manko-Novikov: the reference's formulas form their exponents' arguments as differences
+    # of O(1) terms that cancel to O(1/x^3), ~1e-15 absolute in FP64; central differences at
+    # h = 1e-5 turn that into ~3e-7 of the largest Christoffel symbol at r ~ 10^3
+    assert worst < (1e-6 if metric == 4 else 1e-7), worst
 
 
-def test_no_analytic_plugin_for_manko_novikov(engine_lib):
+def test_unknown_metric_has_no_analytic_plugin(engine_lib):
     p = np.array([0.94, 13.0, 0, 0, 0, 0.0])
     x = np.array([0.0, 10.0, 1.0, 0.0])
     g = np.zeros(64)
-    assert engine_lib.foort_metric_christoffel(4, p.ctypes.data, 0, x.ctypes.data, g.ctypes.data) == -6
+    assert engine_lib.foort_metric_christoffel(7, p.ctypes.data, 0, x.ctypes.data, g.ctypes.data) == -6
 
 
 def test_fp32_acceleration_accuracy(tmp_path):
@@ -62,6 +65,12 @@ def test_fp32_acceleration_accuracy(tmp_path):
         name, p50, p90, p99, mx = line.split()
         p50, p99, mx = float(p50), float(p99), float(mx)
         print(line)
+        if name.startswith("manko_novikov"):
+            # its derivatives of ratios that tend to constants far out (f = e^(2 psi) AA/BB)
+            # lose digits in FP32 dual arithmetic where the generated plugins cancel
+            # symbolically: a few times the other metrics' error
+            assert p50 < 6e-7 and p99 < 1e-5 and mx < 5e-4, line
+            continue
         # FP32 has 6e-8 unit roundoff; a few operations deep the acceleration keeps ~1e-7
         assert p50 < 3e-7 and p99 < 3e-6 and mx < 1e-4, line
         if name == "ff_sincos":

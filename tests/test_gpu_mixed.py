@@ -179,11 +179,35 @@ def test_mixed_budget_and_cancel_paths(eng):
     assert np.any(res["err"] & (abi.ERR_BUDGET | abi.ERR_UNFINISHED))
 
 
-def test_unsupported_metric_for_mixed(eng):
-    d = workloads.base_desc(abi.PREC_MIXED)
-    d.metric_id = abi.METRIC_MANKO_NOVIKOV
-    keep = abi.attach_images(d, [abi.make_image((0.9, 1.0))])
-    with pytest.raises(eng.FoortError) as e:
-        eng.Engine(d)
-    assert e.value.code == abi.FOORT_E_UNSUPPORTED
+# Manko-Novikov (a, alpha3): the reference's Test.cfg value alpha3 = 13, its default 5,
+# and a mild 1
+MN_SETS = {"alpha3_13": (0.94, 13.0), "alpha3_5": (0.9, 5.0), "alpha3_1": (0.7, 1.0)}
+
+
+@pytest.mark.parametrize("name,integ", [("alpha3_13", abi.INTEGRATOR_RK4), ("alpha3_5", abi.INTEGRATOR_RK4),
+                                        ("alpha3_1", abi.INTEGRATOR_RK4), ("alpha3_5", abi.INTEGRATOR_VERLET)])
+def test_mixed_manko_novikov(eng, oracle_mod, name, integ):
+    """Manko-Novikov seen at 63 deg on a 48^2 screen: the mixed kernel (FP32 outside the
+    radius where the metric's exponents exceed 8, FP64 inside) against the FP64 kernel,
+    as for the other metrics."""
+    d = workloads.base_desc()
+    d.metric_id, d.integrator_id = abi.METRIC_MANKO_NOVIKOV, integ
+    d.term_flags |= abi.TERM_THETA_SINGULARITY
+    d.timeout_max_steps = 20000
+    d.diag_flags = abi.DIAG_FOUR_COLOR_SCREEN | abi.DIAG_EQUATORIAL_PASSES | abi.DIAG_CLOSEST_RADIUS
+    keep = abi.attach_images(d, [abi.make_image(MN_SETS[name], r=1000.0, theta=1.1, half_width=12.0)])
+    px = abi.square_pixels(48)
+    res, sm = run(eng, d, px, abi.PREC_MIXED)
+    r64, s64 = run(eng, d, px, abi.PREC_FP64)
+    d.precision = abi.PREC_FP64
+    mism = parity.discrete_mismatch(res, r64)
+    unexplained = parity.explain_mismatches(oracle_mod, d, px, res, mism)
+    same = (~mism) & (res["steps"] == r64["steps"])
+    s = parity.summarize(parity.endpoint_rel_err(res[same], r64[same]))
+    print(f"MN {name} integrator={integ}: agreement {1 - mism.mean():.4f}, same steps {same.mean():.4f}, "
+          f"endpoint {s}, FP64 share of right-hand sides {sm['fp64_steps'] / max(1, sm['rhs_evals']):.3f}, "
+          f"speed-up {s64['kernel_ms'] / sm['kernel_ms']:.1f}x")
+    assert len(unexplained) == 0, unexplained
+    assert 1 - mism.mean() >= parity.MIN_DISCRETE_AGREEMENT
+    assert s["median"] < MIXED_MEDIAN_TOL and s["p90"] < MIXED_P90_TOL, s
     del keep
