@@ -140,19 +140,28 @@ RL_SETS = {"lorenzo": (0.3556562853309941, 0.2969060968239216, 3.057664971085168
            "default": (1.0, 0.5, 2.0, 2.0)}
 
 
-@pytest.mark.parametrize("name,rlog,integ", [("lorenzo", 0, abi.INTEGRATOR_RK4), ("lorenzo", 1, abi.INTEGRATOR_RK4),
-                                             ("m1", 0, abi.INTEGRATOR_RK4), ("default", 0, abi.INTEGRATOR_RK4),
-                                             ("lorenzo", 0, abi.INTEGRATOR_VERLET)])
-def test_mixed_rasheed_larsen(eng, oracle_mod, name, rlog, integ):
-    """Rasheed-Larsen seen at 63 deg on a 48^2 screen: the mixed kernel's discrete
-    outcomes against the FP64 kernel (disagreements explained by the oracle), and its
-    endpoint error against the FP64 kernel within the mixed tolerances."""
+# screens: (inclination, half-width). 63 deg and 12 M mostly see weakly bent rays; 80 deg
+# and 5 M put most pixels on the strongly lensed rays around the shadow.
+VIEWS = {"wide": (1.1, 12.0), "shadow": (1.3962634016, 5.0)}
+
+
+@pytest.mark.parametrize("name,rlog,integ,view", [("lorenzo", 0, abi.INTEGRATOR_RK4, "wide"),
+                                                  ("lorenzo", 1, abi.INTEGRATOR_RK4, "wide"),
+                                                  ("m1", 0, abi.INTEGRATOR_RK4, "wide"),
+                                                  ("default", 0, abi.INTEGRATOR_RK4, "wide"),
+                                                  ("lorenzo", 0, abi.INTEGRATOR_VERLET, "wide"),
+                                                  ("lorenzo", 0, abi.INTEGRATOR_RK4, "shadow")])
+def test_mixed_rasheed_larsen(eng, oracle_mod, name, rlog, integ, view):
+    """Rasheed-Larsen on a 48^2 screen: the mixed kernel's discrete outcomes against the
+    FP64 kernel (disagreements explained by the oracle), and its endpoint error against
+    the FP64 kernel within the mixed tolerances."""
     d = workloads.base_desc()
     d.metric_id, d.rlog, d.integrator_id = abi.METRIC_RASHEED_LARSEN, rlog, integ
     d.term_flags |= abi.TERM_THETA_SINGULARITY
     d.timeout_max_steps = 20000
     d.diag_flags = abi.DIAG_FOUR_COLOR_SCREEN | abi.DIAG_EQUATORIAL_PASSES | abi.DIAG_CLOSEST_RADIUS
-    keep = abi.attach_images(d, [abi.make_image(RL_SETS[name], r=1000.0, theta=1.1, half_width=12.0)])
+    inc, hw = VIEWS[view]
+    keep = abi.attach_images(d, [abi.make_image(RL_SETS[name], r=1000.0, theta=inc, half_width=hw)])
     px = abi.square_pixels(48)
     res, sm = run(eng, d, px, abi.PREC_MIXED)
     r64, s64 = run(eng, d, px, abi.PREC_FP64)
@@ -161,7 +170,7 @@ def test_mixed_rasheed_larsen(eng, oracle_mod, name, rlog, integ):
     unexplained = parity.explain_mismatches(oracle_mod, d, px, res, mism)
     same = (~mism) & (res["steps"] == r64["steps"])
     s = parity.summarize(parity.endpoint_rel_err(res[same], r64[same], rlog=bool(rlog)))
-    print(f"RL {name} rlog={rlog} integrator={integ}: agreement {1 - mism.mean():.4f}, same steps "
+    print(f"RL {name} rlog={rlog} integrator={integ} {view}: agreement {1 - mism.mean():.4f}, same steps "
           f"{same.mean():.4f}, endpoint {s}, speed-up {s64['kernel_ms'] / sm['kernel_ms']:.1f}x")
     assert len(unexplained) == 0, unexplained
     assert 1 - mism.mean() >= parity.MIN_DISCRETE_AGREEMENT
@@ -184,18 +193,22 @@ def test_mixed_budget_and_cancel_paths(eng):
 MN_SETS = {"alpha3_13": (0.94, 13.0), "alpha3_5": (0.9, 5.0), "alpha3_1": (0.7, 1.0)}
 
 
-@pytest.mark.parametrize("name,integ", [("alpha3_13", abi.INTEGRATOR_RK4), ("alpha3_5", abi.INTEGRATOR_RK4),
-                                        ("alpha3_1", abi.INTEGRATOR_RK4), ("alpha3_5", abi.INTEGRATOR_VERLET)])
-def test_mixed_manko_novikov(eng, oracle_mod, name, integ):
-    """Manko-Novikov seen at 63 deg on a 48^2 screen: the mixed kernel (FP32 outside the
-    radius where the metric's exponents exceed 8, FP64 inside) against the FP64 kernel,
-    as for the other metrics."""
+@pytest.mark.parametrize("name,integ,view", [("alpha3_13", abi.INTEGRATOR_RK4, "wide"),
+                                             ("alpha3_5", abi.INTEGRATOR_RK4, "wide"),
+                                             ("alpha3_1", abi.INTEGRATOR_RK4, "wide"),
+                                             ("alpha3_5", abi.INTEGRATOR_VERLET, "wide"),
+                                             ("alpha3_13", abi.INTEGRATOR_RK4, "shadow")])
+def test_mixed_manko_novikov(eng, oracle_mod, name, integ, view):
+    """Manko-Novikov on a 48^2 screen: the mixed kernel (FP32 outside the radius where the
+    metric's exponents exceed 8, FP64 inside) against the FP64 kernel, as for the other
+    metrics."""
     d = workloads.base_desc()
     d.metric_id, d.integrator_id = abi.METRIC_MANKO_NOVIKOV, integ
     d.term_flags |= abi.TERM_THETA_SINGULARITY
     d.timeout_max_steps = 20000
     d.diag_flags = abi.DIAG_FOUR_COLOR_SCREEN | abi.DIAG_EQUATORIAL_PASSES | abi.DIAG_CLOSEST_RADIUS
-    keep = abi.attach_images(d, [abi.make_image(MN_SETS[name], r=1000.0, theta=1.1, half_width=12.0)])
+    inc, hw = VIEWS[view]
+    keep = abi.attach_images(d, [abi.make_image(MN_SETS[name], r=1000.0, theta=inc, half_width=hw)])
     px = abi.square_pixels(48)
     res, sm = run(eng, d, px, abi.PREC_MIXED)
     r64, s64 = run(eng, d, px, abi.PREC_FP64)
@@ -204,7 +217,7 @@ def test_mixed_manko_novikov(eng, oracle_mod, name, integ):
     unexplained = parity.explain_mismatches(oracle_mod, d, px, res, mism)
     same = (~mism) & (res["steps"] == r64["steps"])
     s = parity.summarize(parity.endpoint_rel_err(res[same], r64[same]))
-    print(f"MN {name} integrator={integ}: agreement {1 - mism.mean():.4f}, same steps {same.mean():.4f}, "
+    print(f"MN {name} integrator={integ} {view}: agreement {1 - mism.mean():.4f}, same steps {same.mean():.4f}, "
           f"endpoint {s}, FP64 share of right-hand sides {sm['fp64_steps'] / max(1, sm['rhs_evals']):.3f}, "
           f"speed-up {s64['kernel_ms'] / sm['kernel_ms']:.1f}x")
     assert len(unexplained) == 0, unexplained
