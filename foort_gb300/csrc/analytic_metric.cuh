@@ -26,14 +26,16 @@ struct G5T {
 // reciprocal r0 refined by one Newton-Raphson step, r1 = r0 + r0 (1 - x r0), which
 // squares r0's relative error (~2^-23) away and leaves the final FMA's rounding: within
 // one ulp, in three instructions and without the branches of a correctly rounded
-// reciprocal (which sit on the critical path of every right-hand side). Infinite r0
-// (x = 0) is passed through, where the refinement would give NaN.
+// reciprocal (which sit on the critical path of every right-hand side). For x = 0 it
+// gives NaN where 1/x is infinite: the factors are r - r_+, r - r_-, sin(theta), Sigma,
+// r and the like, exactly 0 only on a horizon, a pole or the origin, where the state
+// turns non-finite with either value. Passing the infinity through cost C2 1.2 % on
+// GB300.
 FOORT_HD float rcp(float x) {
 #ifdef __CUDA_ARCH__
     float r0;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(x));
-    const float r1 = __fmaf_rn(r0, __fmaf_rn(-x, r0, 1.0f), r0);
-    return isinf(r0) ? r0 : r1;
+    return __fmaf_rn(r0, __fmaf_rn(-x, r0, 1.0f), r0);
 #else
     return 1.0f / x;
 #endif
