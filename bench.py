@@ -49,7 +49,7 @@ SINCOS_PER_STEP = {("kerr", "rk4"): 20, ("johannsen", "rk4"): 20, ("johannsen", 
 OPS_PER_EXTRA_VERLET_RHS = 380
 # DRAM traffic per geodesic of the mixed kernel (dram__bytes_read.sum + dram__bytes_write.sum
 # of one ncu capture divided by its geodesics; profiles/integrate_mixed_pair_kernel_c2.md)
-DRAM_BYTES_PER_GEODESIC = {("kerr", "rk4"): 131.2}
+DRAM_BYTES_PER_GEODESIC = {("kerr", "rk4"): 121.1}
 
 
 from foort_gb300.multirank import dist_env  # noqa: E402
