@@ -457,10 +457,11 @@ def main():
     e2e = {"value": world * n_geod / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
            "ms_per_step": t_e2e * 1e3}
 
-    # ---- FP64 plain kernel on the same pixels (rank 0 of an N=1 run by default)
+    # ---- FP64 plain kernel on the same pixels (N = 1 only: under torchrun the other GPUs
+    # would wait for it)
     fp64 = None
     acc = None
-    if not args.no_fp64 and rank == 0:
+    if not args.no_fp64 and world == 1:
         wl64 = workload(args.workload, abi.PREC_FP64, args.iteration_pixels)
         with foort_gb300.Engine(wl64.desc) as e:
             e.integrate(rounds[-1][:256])  # warm-up
@@ -507,9 +508,9 @@ def main():
                 "launch_ms": big_ms, "steps_per_launch": big_steps,
                 "fp64_peak_tflops": peaks[1]}
 
-    # ---- CPU baseline: oracle restatement (-Ofast, all host threads) on a sample
+    # ---- CPU baseline: oracle restatement (-Ofast, all host threads) on a sample (N = 1 only)
     cpu = None
-    if not args.no_cpu and rank == 0:
+    if not args.no_cpu and world == 1:
         nthreads = os.cpu_count() or 1
         wl_cpu = workload(args.workload, abi.PREC_FP64, args.iteration_pixels)
         rate, n, dt, _ = cpu_sample_rate(wl_cpu, np.concatenate(rounds), args.cpu_seconds or 15.0, nthreads)
