@@ -16,7 +16,8 @@ One step = every round of the workload:
          foort_gpu_integrate (H2D of the pixels, kernel, D2H of the results) ->
          foort_mesh_set_results -> foort_mesh_end_current_loop, every round.
 N > 1 (torchrun): every rank integrates its own copy of the workload (weak scaling,
-no collective on the data path); times are the max over ranks.
+no collective on the data path); times are the max over ranks. The FP64 and CPU legs
+run at N = 1 only.
 --impl reference: the reference's algorithm on the host cores (the oracle's
 restatement built with the reference's -Ofast flags; the reference itself only builds
 where its sources are), on a bounded seeded sample of the pixels the reference's own
