@@ -91,3 +91,88 @@ def test_generated_plugins_match_the_generator(tmp_path):
     with open(os.path.join(ROOT, "foort_gb300", "csrc", "gen_christoffel.inc")) as f:
         committed = f.read()
     assert out.read_text() == committed
+
+
+def _mn_gdd_mp(mp, a, a3, r, th):
+    """Manko-Novikov g_dd (tt, tp, rr, hh, pp) from the reference's formulas
+    (Metric.cpp:511-566), in mpmath arithmetic (test-only restatement)."""
+    k = mp.sqrt(1 - a * a)
+    al = (-1 + mp.sqrt(1 - a * a)) / a
+    x, y = (r - 1) / k, mp.cos(th)
+    s = mp.sin(th)
+    R = mp.sqrt(x * x + y * y - 1)
+    t = x * y / R
+    P1, P2 = t, (3 * t * t - 1) / 2
+    P3, P4 = (5 * t ** 3 - 3 * t) / 2, (35 * t ** 4 - 30 * t * t + 3) / 8
+    aa = -al * mp.exp(2 * a3 * (1 - (x - y) * (1 / R + P1 / R ** 2 + P2 / R ** 3 + P3 / R ** 4)))
+    bb = al * mp.exp(2 * a3 * (-1 + (x + y) * (1 / R - P1 / R ** 2 + P2 / R ** 3 - P3 / R ** 4)))
+    AA = (x * x - 1) * (1 + aa * bb) ** 2 - (1 - y * y) * (bb - aa) ** 2
+    BB = (x + 1 + (x - 1) * aa * bb) ** 2 + ((1 + y) * aa + (1 - y) * bb) ** 2
+    CC = (x * x - 1) * (1 + aa * bb) * (bb - aa - y * (aa + bb)) + (1 - y * y) * (bb - aa) * (1 + aa * bb + x * (1 - aa * bb))
+    psi = a3 * P3 / R ** 4
+    gp = 2 * a3 * a3 * (P4 * P4 - P3 * P3) / R ** 8 + 2 * a3 * (-y + x * P1 / R - y * P2 / R ** 2 + x * P3 / R ** 3) / R
+    f = mp.exp(2 * psi) * AA / BB
+    e2g = mp.exp(2 * gp) * AA / ((x * x - y * y) * (1 - al * al) ** 2)
+    om = 2 * k * mp.exp(-2 * psi) * CC / AA - 4 * k * al / (1 - al * al)
+    rho2 = (r - 1) ** 2 - k * k * y * y
+    de = (r - 1) ** 2 - k * k
+    g22 = e2g * rho2 / f
+    return [-f, om * f, g22 / de, g22, -f * om * om + de * s * s / f]
+
+
+@pytest.mark.parametrize("params", [(0.94, 13.0), (0.9, 5.0), (0.7, 1.0)])
+def test_manko_novikov_derivatives_near_the_horizon(engine_lib, params):
+    """The plugin's FP64 derivatives (the mixed kernel's FP64 right-hand side near the
+    horizon) against 50-digit central differences of the reference's formulas, from
+    r_+ + 0.01 to r_+ + 1.5, where FP64 finite differences cannot resolve them."""
+    mp = pytest.importorskip("mpmath").mp
+    mp.dps = 50
+    a, a3 = params
+    rp = 1 + np.sqrt(1 - a * a)
+    p = np.zeros(6)
+    p[:2] = params
+    rng = np.random.default_rng(3)
+    worst = 0.0
+    checked = 0
+    for _ in range(40):
+        r = rp + 10 ** rng.uniform(-2, np.log10(1.5))
+        th = rng.uniform(0.2, 2.9)
+        x = np.array([0.0, r, th, 0.0])
+        g = np.zeros(64)
+        assert engine_lib.foort_metric_christoffel(4, p.ctypes.data, 0, x.ctypes.data, g.ctypes.data) == 0
+        if not np.all(np.isfinite(g)):
+            continue  # the metric itself leaves FP64's range there
+        h = mp.mpf("1e-20")
+        rm, tm = mp.mpf(r), mp.mpf(th)
+        d_r = [(u - v) / (2 * h) for u, v in zip(_mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm + h, tm),
+                                                 _mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm - h, tm))]
+        d_t = [(u - v) / (2 * h) for u, v in zip(_mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm, tm + h),
+                                                 _mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm, tm - h))]
+        gd = _mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm, tm)
+        if not all(mp.mpf("1e-290") < abs(v) < mp.mpf("1e290") for v in gd):
+            continue  # the metric leaves FP64's range there
+        # Christoffel symbols from the high-precision derivatives (the engine's layout);
+        # the (t, phi) block's determinant is -Delta sin^2 exactly (formed directly: as
+        # g_tt g_phiphi - g_tphi^2 it cancels beyond even 50 digits where the components
+        # are large)
+        kk = 1 - mp.mpf(a) ** 2
+        det = -((rm - 1) ** 2 - kk) * mp.sin(tm) ** 2
+        gu = {"tt": float(gd[4] / det), "tp": float(-gd[1] / det), "pp": float(gd[0] / det),
+              "rr": float(1 / gd[2]), "hh": float(1 / gd[3])}
+        D = np.zeros((4, 4, 4))  # D[c][i][j] = d_c g_ij
+        for c, dv in ((1, d_r), (2, d_t)):
+            vt, vtp, vr, vh, vp = [float(v) for v in dv]
+            D[c][0][0], D[c][0][3], D[c][3][0], D[c][1][1], D[c][2][2], D[c][3][3] = vt, vtp, vtp, vr, vh, vp
+        G = np.zeros((4, 4))
+        G[0][0], G[0][3], G[3][0], G[3][3], G[1][1], G[2][2] = gu["tt"], gu["tp"], gu["tp"], gu["pp"], gu["rr"], gu["hh"]
+        want = np.zeros(64)
+        for mu in range(4):
+            for nu in range(4):
+                for rho in range(4):
+                    want[16 * mu + 4 * nu + rho] = 0.5 * sum(
+                        G[mu][sg] * (D[nu][rho][sg] + D[rho][nu][sg] - D[sg][nu][rho]) for sg in range(4))
+        worst = max(worst, np.abs(g - want).max() / np.abs(want).max())
+        checked += 1
+    print(f"{params}: {checked} points, worst relative difference {worst:.2e}")
+    assert checked >= 20, checked
+    assert worst < 1e-10, worst
