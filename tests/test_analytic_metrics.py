@@ -120,17 +120,62 @@ def _mn_gdd_mp(mp, a, a3, r, th):
     return [-f, om * f, g22 / de, g22, -f * om * om + de * s * s / f]
 
 
-@pytest.mark.parametrize("params", [(0.94, 13.0), (0.9, 5.0), (0.7, 1.0)])
-def test_manko_novikov_derivatives_near_the_horizon(engine_lib, params):
-    """The plugin's FP64 derivatives (the mixed kernel's FP64 right-hand side near the
-    horizon) against 50-digit central differences of the reference's formulas, from
-    r_+ + 0.01 to r_+ + 1.5, where FP64 finite differences cannot resolve them."""
+def _gdd_mp(mp, metric, q, r, th):
+    """g_dd (tt, tp, rr, hh, pp) of Kerr (0), Rasheed-Larsen (2) and Johannsen (3) from the
+    reference's formulas (Metric.cpp:131-159, :273-316, :409-440), in mpmath arithmetic;
+    Manko-Novikov (4) by _mn_gdd_mp. Test-only restatements."""
+    s, c = mp.sin(th), mp.cos(th)
+    if metric == 4:
+        return _mn_gdd_mp(mp, q[0], q[1], r, th)
+    if metric == 0:
+        a = q[0]
+        sig = r * r + a * a * c * c
+        de = r * r + a * a - 2 * r
+        A = (r * r + a * a) ** 2 - de * a * a * s * s
+        return [-(1 - 2 * r / sig), -2 * a * r * s * s / sig, sig / de, sig, A / sig * s * s]
+    if metric == 3:
+        a, a13, a22, a52, e3 = q[:5]
+        A1, A2, A5 = 1 + a13 / r ** 3, 1 + a22 / r ** 2, 1 + a52 / r ** 2
+        rho2 = r * r + a * a * c * c + e3 / r
+        de = r * r + a * a - 2 * r
+        den = (r * r + a * a) * A1 - a * a * A2 * s * s
+        ra = (r * r + a * a) * A1
+        return [-rho2 * (de - a * a * A2 * A2 * s * s) / den ** 2,
+                -a * ((r * r + a * a) * A1 * A2 - de) * rho2 * s * s / den ** 2,
+                rho2 / (de * A5), rho2, rho2 * s * s * (ra * ra - a * a * de * s * s) / den ** 2]
+    # Rasheed-Larsen, parameters rescaled to M = 1 (Metric.cpp:244-252)
+    m0, a0, p0, q0 = q[:4]
+    sc = (p0 + q0) / 4
+    m, a, p, qq = m0 / sc, a0 / sc, p0 / sc, q0 / sc
+    de = r * r + a * a - 2 * r * m
+    H3 = r * r - 2 * r * m + a * a * c * c
+    Bp = mp.sqrt(p * qq) * a * s * s * (((p * qq + 4 * m * m) * r - m * (p - 2 * m) * (qq - 2 * m))
+                                        / (2 * m * (p + qq) * H3))
+    W = mp.sqrt((p * p - 4 * m * m) * (qq * qq - 4 * m * m))
+    H1 = r * r + a * a * c * c + r * (p - 2 * m) + p / (p + qq) * ((p - 2 * m) * (qq - 2 * m) / 2) \
+        - p / (2 * m * (p + qq)) * W * a * c
+    H2 = r * r + a * a * c * c + r * (qq - 2 * m) + qq / (p + qq) * ((p - 2 * m) * (qq - 2 * m) / 2) \
+        + qq / (2 * m * (p + qq)) * W * a * c
+    S = mp.sqrt(H1 * H2)
+    return [-H3 / S, -H3 * Bp / S, S / de, S, -H3 * Bp * Bp / S + S * de * s * s / H3]
+
+
+NEAR_CASES = [(0, (0.99,)), (0, (0.5,)), (3, (0.9, -0.6, 0, 0, 0)), (3, (0.8, 1.0, 0.5, 0.2, 0.1)),
+              (2, RL_LORENZO), (2, RL_M1), (4, (0.94, 13.0)), (4, (0.9, 5.0)), (4, (0.7, 1.0))]
+
+
+@pytest.mark.parametrize("metric,params", NEAR_CASES)
+def test_plugin_derivatives_near_the_horizon(engine_lib, metric, params):
+    """The plugins' FP64 Christoffel symbols (foort_metric_christoffel; the mixed kernel's
+    FP64 right-hand side uses the same code) against 50-digit central differences of the
+    reference's formulas, from r_+ + 0.01 to r_+ + 1.5, where FP64 finite differences
+    cannot resolve the derivatives."""
     mp = pytest.importorskip("mpmath").mp
     mp.dps = 50
-    a, a3 = params
-    rp = 1 + np.sqrt(1 - a * a)
     p = np.zeros(6)
-    p[:2] = params
+    p[:len(params)] = params
+    rp = engine_lib.foort_horizon_radius(metric, p.ctypes.data)
+    qm = [mp.mpf(v) for v in p]
     rng = np.random.default_rng(3)
     worst = 0.0
     checked = 0
@@ -139,30 +184,30 @@ def test_manko_novikov_derivatives_near_the_horizon(engine_lib, params):
         th = rng.uniform(0.2, 2.9)
         x = np.array([0.0, r, th, 0.0])
         g = np.zeros(64)
-        assert engine_lib.foort_metric_christoffel(4, p.ctypes.data, 0, x.ctypes.data, g.ctypes.data) == 0
+        assert engine_lib.foort_metric_christoffel(metric, p.ctypes.data, 0, x.ctypes.data, g.ctypes.data) == 0
         if not np.all(np.isfinite(g)):
             continue  # the metric itself leaves FP64's range there
-        h = mp.mpf("1e-20")
         rm, tm = mp.mpf(r), mp.mpf(th)
-        d_r = [(u - v) / (2 * h) for u, v in zip(_mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm + h, tm),
-                                                 _mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm - h, tm))]
-        d_t = [(u - v) / (2 * h) for u, v in zip(_mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm, tm + h),
-                                                 _mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm, tm - h))]
-        gd = _mn_gdd_mp(mp, mp.mpf(a), mp.mpf(a3), rm, tm)
-        if not all(mp.mpf("1e-290") < abs(v) < mp.mpf("1e290") for v in gd):
-            continue  # the metric leaves FP64's range there
-        # Christoffel symbols from the high-precision derivatives (the engine's layout);
-        # the (t, phi) block's determinant is -Delta sin^2 exactly (formed directly: as
-        # g_tt g_phiphi - g_tphi^2 it cancels beyond even 50 digits where the components
-        # are large)
-        kk = 1 - mp.mpf(a) ** 2
-        det = -((rm - 1) ** 2 - kk) * mp.sin(tm) ** 2
+        gd = _gdd_mp(mp, metric, qm, rm, tm)
+        if not all(mp.mpf("1e-290") < abs(v) < mp.mpf("1e290") for v in gd if v != 0):
+            continue
+        h = mp.mpf("1e-20")
+        d_r = [(u - v) / (2 * h) for u, v in zip(_gdd_mp(mp, metric, qm, rm + h, tm), _gdd_mp(mp, metric, qm, rm - h, tm))]
+        d_t = [(u - v) / (2 * h) for u, v in zip(_gdd_mp(mp, metric, qm, rm, tm + h), _gdd_mp(mp, metric, qm, rm, tm - h))]
+        # inverse of the (t, phi) block; Manko-Novikov's determinant is -Delta sin^2 exactly
+        # (as g_tt g_phiphi - g_tphi^2 it cancels beyond even 50 digits where its
+        # components are large)
+        if metric == 4:
+            det = -((rm - 1) ** 2 - (1 - qm[0] ** 2)) * mp.sin(tm) ** 2
+        else:
+            det = gd[0] * gd[4] - gd[1] * gd[1]
         gu = {"tt": float(gd[4] / det), "tp": float(-gd[1] / det), "pp": float(gd[0] / det),
               "rr": float(1 / gd[2]), "hh": float(1 / gd[3])}
         D = np.zeros((4, 4, 4))  # D[c][i][j] = d_c g_ij
-        for c, dv in ((1, d_r), (2, d_t)):
+        for cdir, dv in ((1, d_r), (2, d_t)):
             vt, vtp, vr, vh, vp = [float(v) for v in dv]
-            D[c][0][0], D[c][0][3], D[c][3][0], D[c][1][1], D[c][2][2], D[c][3][3] = vt, vtp, vtp, vr, vh, vp
+            D[cdir][0][0], D[cdir][0][3], D[cdir][3][0], D[cdir][1][1], D[cdir][2][2], D[cdir][3][3] = \
+                vt, vtp, vtp, vr, vh, vp
         G = np.zeros((4, 4))
         G[0][0], G[0][3], G[3][0], G[3][3], G[1][1], G[2][2] = gu["tt"], gu["tp"], gu["tp"], gu["pp"], gu["rr"], gu["hh"]
         want = np.zeros(64)
@@ -173,6 +218,6 @@ def test_manko_novikov_derivatives_near_the_horizon(engine_lib, params):
                         G[mu][sg] * (D[nu][rho][sg] + D[rho][nu][sg] - D[sg][nu][rho]) for sg in range(4))
         worst = max(worst, np.abs(g - want).max() / np.abs(want).max())
         checked += 1
-    print(f"{params}: {checked} points, worst relative difference {worst:.2e}")
+    print(f"metric {metric} {params}: {checked} points, worst relative difference {worst:.2e}")
     assert checked >= 20, checked
     assert worst < 1e-10, worst
