@@ -11,10 +11,16 @@ kernel on the same pixels and the endpoint error between the two.
 One step = every round of the workload:
   value  pixel lists of all rounds resident in HBM, one persistent-kernel launch per
          round through foort_gpu_integrate_async on one stream; CUDA events on that
-         stream around each step; L2 flushed (256 MB write) between steps;
+         stream around each step; L2 flushed (256 MB write) between steps; the launch
+         shape of each round chosen by the engine's autotuner (foort_gpu_autotune) in
+         the first warm-up step;
   e2e    the full run through the public C ABI from pinned host memory: host mesh ->
          foort_gpu_integrate (H2D of the pixels, kernel, D2H of the results) ->
          foort_mesh_set_results -> foort_mesh_end_current_loop, every round.
+Accuracy (N = 1): the plain FP64 kernel (the reference's finite differences) on the same
+rounds, timed for the speed-up; the FP64-analytic oracle (every step in FP64 with the
+mixed kernel's derivatives) on all pixels; per-pixel condition numbers from two shifted
+launches; error reports of mixed and plain FP64 against the oracle (foort_gb300.accuracy).
 N > 1 (torchrun): every rank integrates its own copy of the workload (weak scaling,
 no collective on the data path); times are the max over ranks. The FP64 and CPU legs
 run at N = 1 only.
@@ -48,9 +54,16 @@ UNIT = "geodesics/s"
 OPS_PER_STEP = {("kerr", "rk4"): 1130, ("johannsen", "rk4"): 1650, ("johannsen", "verlet"): 830}
 SINCOS_PER_STEP = {("kerr", "rk4"): 20, ("johannsen", "rk4"): 20, ("johannsen", "verlet"): 10}
 OPS_PER_EXTRA_VERLET_RHS = 380
-# DRAM traffic per geodesic of the mixed kernel (dram__bytes_read.sum + dram__bytes_write.sum
-# of one ncu capture divided by its geodesics; profiles/integrate_mixed_pair_kernel_c2.md)
+# DRAM traffic per geodesic of the mixed kernel: dram__bytes_read.sum + dram__bytes_write.sum
+# of one ncu capture of the two-lane kernel on a 6,000-pixel sample of the C2 grid, divided
+# by its geodesics
 DRAM_BYTES_PER_GEODESIC = {("kerr", "rk4"): 121.1}
+# Executed thread instructions per geodesic step of the mixed kernel (ncu
+# smsp__inst_executed x 32 / steps on the same capture): two lanes of ~1,000 each, or one
+# lane of ~1,320. With the GPU's issue rate (one warp instruction per cycle on each of its
+# 4 x 152 sub-partitions) they give the fraction of issue slots the path fills.
+EXEC_INSTR_PER_STEP = {("kerr", "rk4", 2): 2000, ("kerr", "rk4", 1): 1320}
+SUBPARTITIONS = 4
 
 
 from foort_gb300.multirank import dist_env  # noqa: E402
@@ -305,16 +318,37 @@ def config_block(wl, args, side=None, rounds=None, geod=None):
     return c
 
 
-def endpoint_stats(mixed, fp64, rlog):
-    from foort_gb300 import accuracy
-    mism = accuracy.discrete_mismatch(mixed, fp64)
-    same = (~mism) & (mixed["steps"] == fp64["steps"])
-    err = accuracy.endpoint_rel_err(mixed[same], fp64[same], rlog=rlog)
-    s = accuracy.summarize(err)
-    s["frac_le_1e-6"] = float(np.mean(err <= 1e-6)) if len(err) else None
-    s["discrete_agreement"] = float(1.0 - mism.mean())
-    s["same_step_count"] = float(same.mean())
-    return s
+def accuracy_legs(fg, args, wl, px_all, mixed_all, res64_all):
+    """Endpoint errors against the FP64-analytic oracle (every step in FP64 with the mixed
+    kernel's analytic derivatives): of the mixed kernel, and of the plain FP64 kernel (the
+    reference's finite differences); and of the mixed kernel against the plain FP64 kernel.
+    Every pixel counts (a discrete disagreement as an infinite error); each report splits
+    off the well-conditioned pixels and gives the backward error err / kappa, with the
+    condition numbers kappa from two launches of the mixed kernel at screen points shifted
+    by ~1e-6 (foort_gb300.accuracy)."""
+    from foort_gb300 import abi, accuracy
+    rlog = bool(wl.desc.rlog)
+    wla = workload(args.workload, abi.PREC_FP64_ANALYTIC, args.iteration_pixels)
+    with fg.Engine(wla.desc) as e:
+        e.integrate(px_all[:128])
+        resa = e.integrate(px_all)
+        ta = e.stats()["kernel_ms"]
+    grids = px_all["grid"].astype(np.int64)
+    K, _ = accuracy.shift_refinement(int(grids.max()))
+    step = 1.0 / (K * (grids - 1))
+    with fg.Engine(wl.desc) as e:
+        shifted = [e.integrate(accuracy.shifted_pixels(px_all, K, ax)) for ax in (0, 1)]
+    kappa = accuracy.condition_numbers(mixed_all, shifted, step, rlog=rlog)
+    rep = {
+        "oracle": "FP64-analytic: every step in FP64 with the mixed kernel's analytic derivatives "
+                  f"({len(px_all)} pixels in one launch, {ta:.0f} ms)",
+        "kappa": f"endpoint change per unit screen shift, from shifts of {float(np.median(step)):.2e} of the screen; "
+                 f"well-conditioned: kappa <= {accuracy.KAPPA_WELL:g}",
+        "mixed_vs_fp64_analytic": accuracy.error_report(accuracy.endpoint_err_all(mixed_all, resa, rlog), kappa),
+        "fp64_vs_fp64_analytic": accuracy.error_report(accuracy.endpoint_err_all(res64_all, resa, rlog), kappa),
+        "mixed_vs_fp64": accuracy.error_report(accuracy.endpoint_err_all(mixed_all, res64_all, rlog), kappa),
+    }
+    return rep
 
 
 def main():
@@ -327,6 +361,8 @@ def main():
     ap.add_argument("--iteration-pixels", type=int, default=None)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="use the built-in launch rule instead of autotuning each round in the first warm-up step")
     ap.add_argument("--cpu-seconds", type=float, default=None,
                     help="host-core seconds of the CPU legs (default: 15 for cpu_baseline, 40 for --impl reference)")
     ap.add_argument("--profile-precision", default="both", choices=["both", "mixed", "fp64"])
@@ -375,14 +411,20 @@ def main():
 
     rhs_per_round = [0] * len(rounds)
     lanes_per_round = [1] * len(rounds)
+    shapes = [None] * len(rounds)
 
-    def device_step(e):
+    def device_step(e, tune=False):
         kms = []
         with torch.cuda.stream(stream):
             for i, (dp, do, r) in enumerate(zip(d_px, d_out, rounds)):
-                e.integrate_async(dp.data_ptr(), len(r), do.data_ptr(), stream.cuda_stream)
-                e.sync()
+                if tune:  # the project autotuner: search, cache, and integrate in the best shape
+                    e.autotune(dp.data_ptr(), len(r), do.data_ptr(), stream.cuda_stream)
+                else:
+                    e.integrate_async(dp.data_ptr(), len(r), do.data_ptr(), stream.cuda_stream)
+                    e.sync()
                 st = e.stats()
+                shapes[i] = {"geodesics": len(r), "block_size": st["block_size"], "lanes": st["lanes_per_geodesic"],
+                             "refill_steps": st["refill_steps"], "poll_steps": st["poll_steps"]}
                 kms.append(st["kernel_ms"])
                 rhs_per_round[i] = st["rhs_evals"]
                 lanes_per_round[i] = st["lanes_per_geodesic"]
@@ -392,8 +434,12 @@ def main():
     peaks = foort_gb300.measure_peaks()
     with foort_gb300.Engine(wl.desc) as e:
         e.set_lanes(args.lanes)
-        for _ in range(args.warmup):
-            device_step(e)
+        t0 = time.perf_counter()
+        for w in range(args.warmup):
+            device_step(e, tune=(w == 0 and not args.no_tune))
+            if w == 0:
+                log(f"[bench] first warm-up step{' (autotuning every round)' if not args.no_tune else ''}: "
+                    f"{time.perf_counter() - t0:.1f}s; shapes {shapes}")
         barrier()
         clocks = ClockSampler(local)
         clocks.start()
@@ -481,32 +527,56 @@ def main():
                 "roofline_fp64": {"achieved": steps64 * OPS_PER_STEP.get(mkind, 1130) / (t64 * 1e-3) / 1e12,
                                   "peak": peaks[1], "unit": "TFLOP/s",
                                   "frac": steps64 * OPS_PER_STEP.get(mkind, 1130) / (t64 * 1e-3) / 1e12 / peaks[1]}}
-        acc = endpoint_stats(np.concatenate(mixed_res), np.concatenate(res64), rlog=bool(wl.desc.rlog))
+        acc = accuracy_legs(foort_gb300, args, wl, np.concatenate(rounds), np.concatenate(mixed_res),
+                            np.concatenate(res64))
 
-    # ---- roofline of the dominant kernel (the mixed kernel's largest launch)
+    # ---- roofline of the dominant kernel: the mixed kernel over all launches of a step
+    # (each round is one launch of it), and its largest launch alone
     n_launch = len(rounds)
     per_launch_ms = [launch_ms[i::n_launch] for i in range(n_launch)]
+    ops = OPS_PER_STEP.get(mkind, 1130)
+
+    def launch_ops(i):
+        st = int(mixed_res[i]["steps"].sum())
+        o = st * ops
+        if mkind[1] == "verlet":  # every velocity iteration beyond the two base evaluations
+            o += OPS_PER_EXTRA_VERLET_RHS * max(0, mixed_rhs[i] - 2 * st)
+        return o, st
+
+    tot_ops = sum(launch_ops(i)[0] for i in range(n_launch))
+    tot_ms = sum(statistics.mean(m) for m in per_launch_ms)
+    achieved = tot_ops / (tot_ms * 1e-3) / 1e12
     big = int(np.argmax([len(r) for r in rounds]))
     big_ms = statistics.mean(per_launch_ms[big])
-    big_rhs = mixed_rhs[big]
-    big_steps = int(mixed_res[big]["steps"].sum())
-    ops = OPS_PER_STEP.get(mkind, 1130)
-    big_ops = big_steps * ops
-    if mkind[1] == "verlet":  # every velocity iteration beyond the two base evaluations
-        big_ops += OPS_PER_EXTRA_VERLET_RHS * max(0, big_rhs - 2 * big_steps)
-    achieved = big_ops / (big_ms * 1e-3) / 1e12
+    big_ops, big_steps = launch_ops(big)
+    # executed instructions: the issue-slot fraction of the whole step
+    instr = sum(int(mixed_res[i]["steps"].sum()) * EXEC_INSTR_PER_STEP.get(mkind + (mixed_lanes[i],), 0)
+                for i in range(n_launch))
+    clock_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    issue_peak = SUBPARTITIONS * torch.cuda.get_device_properties(local).multi_processor_count * clock_mhz * 1e6
+    issue = instr / 32 / (tot_ms * 1e-3)
     # DRAM bytes (read + write) of one launch, from ncu's per-geodesic figure scaled to the
     # launch's geodesics (the capture is a 6,000-geodesic sample of the same grid)
     tpg = DRAM_BYTES_PER_GEODESIC.get(mkind)
     traffic = tpg * len(rounds[big]) if tpg else None
     roofline = {"bound": "alu-fp32", "achieved": achieved, "peak": peaks[0], "unit": "TFLOP/s",
-                "frac": achieved / peaks[0], "traffic": traffic, "traffic_unit": "bytes per launch",
+                "frac": achieved / peaks[0], "traffic": traffic, "traffic_unit": "bytes per launch (largest launch)",
+                "scope": f"all {n_launch} launches of a step: {tot_ops:.4g} reference-formulation operations in "
+                         f"{tot_ms:.1f} ms of kernel time",
                 "ops_per_step": ops, "sincos_per_step": SINCOS_PER_STEP.get(mkind, 20),
                 "peak_source": "FP32 FMA microbenchmark on this GPU (foort_measure_peaks); MEASURED_PEAKS.json "
                                "has no FP32/FP64 entry",
                 "kernel": "integrate_mixed_pair_kernel" if mixed_lanes[big] == 2 else "integrate_mixed_kernel",
-                "lanes_per_geodesic": mixed_lanes[big],
-                "launch_ms": big_ms, "steps_per_launch": big_steps,
+                "lanes_per_geodesic": mixed_lanes,
+                "largest_launch": {"geodesics": len(rounds[big]), "launch_ms": big_ms, "steps": big_steps,
+                                   "achieved": big_ops / (big_ms * 1e-3) / 1e12,
+                                   "frac": big_ops / (big_ms * 1e-3) / 1e12 / peaks[0]},
+                "executed": {"thread_instructions_per_step": {f"{k[2]}-lane": v for k, v in EXEC_INSTR_PER_STEP.items()
+                                                              if k[:2] == mkind},
+                             "warp_instructions_per_s": issue, "issue_peak_per_s": issue_peak,
+                             "issue_frac": issue / issue_peak if instr else None,
+                             "source": "instructions per step from the ncu capture of a 6,000-pixel C2 sample; "
+                                       "issue peak = 4 x SMs x median SM clock"},
                 "fp64_peak_tflops": peaks[1]}
 
     # ---- CPU baseline: oracle restatement (-Ofast, all host threads) on a sample (N = 1 only)
@@ -523,12 +593,13 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "mixed-f32 (FP32 right-hand side; float-float state and decisions)", "data": "synthetic",
-        "config": config_block(wl, args, rounds=len(rounds), geod=n_geod),
+        "config": dict(config_block(wl, args, rounds=len(rounds), geod=n_geod),
+                       autotuned=not args.no_tune, launch_shapes=shapes),
         "geodesics_per_step": world * n_geod, "steps_per_s": world * steps_total / (t_step * 1e-3),
         "gpu_launches": args.steps * len(rounds),
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "fp64": fp64, "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
-        "endpoint_error_vs_fp64": acc,
+        "accuracy": acc,
         "round_sizes": [len(r) for r in rounds],
     }
     if rank == 0:

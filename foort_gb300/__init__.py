@@ -87,6 +87,20 @@ def load():
     lib.foort_geopos_count.argtypes = [C.POINTER(abi.RunDesc), u64, i32, C.POINTER(u64), C.POINTER(u64)]
     lib.foort_output_round_positions.argtypes = [vp, vp, vp, u64, vp, vp]
     lib.foort_gpu_get_desc.argtypes = [vp, C.POINTER(abi.RunDesc)]
+    lib.foort_gpu_autotune.argtypes = [vp, vp, u64, vp, vp, C.POINTER(abi.LaunchShape)]
+    lib.foort_gpu_set_autotune.argtypes = [vp, i32]
+    lib.foort_gpu_launch_shape.argtypes = [vp, u64, C.POINTER(abi.LaunchShape)]
+    lib.foort_tune_bucket.argtypes = [u64]
+    lib.foort_tune_bucket.restype = u32
+    lib.foort_tune_key.argtypes = [C.POINTER(abi.RunDesc), i32, u64, C.c_char_p, u64]
+    lib.foort_tune_put.argtypes = [C.c_char_p, C.POINTER(abi.LaunchShape)]
+    lib.foort_tune_get.argtypes = [C.c_char_p, C.POINTER(abi.LaunchShape)]
+    lib.foort_tune_count.argtypes = []
+    lib.foort_tune_count.restype = u64
+    lib.foort_tune_clear.argtypes = []
+    lib.foort_tune_clear.restype = None
+    lib.foort_tune_save.argtypes = [C.c_char_p]
+    lib.foort_tune_load.argtypes = [C.c_char_p]
     _LIB = lib
     return lib
 
@@ -168,6 +182,23 @@ class Engine:
         """0: chosen per launch; 1 or 2 lanes per geodesic where the kernel has both."""
         self._check(self._lib.foort_gpu_set_lanes(self._ctx, lanes_per_geodesic))
 
+    def autotune(self, d_px, n, d_out, stream=0):
+        """Search launch shapes for n device pixels (foort_gpu_autotune); returns the
+        fastest shape as a dict. d_out then holds the pixels' results."""
+        best = abi.LaunchShape()
+        self._check(self._lib.foort_gpu_autotune(self._ctx, C.c_void_p(d_px), n, C.c_void_p(d_out),
+                                                 C.c_void_p(stream), C.byref(best)))
+        return best.as_dict()
+
+    def set_autotune(self, on=True):
+        self._check(self._lib.foort_gpu_set_autotune(self._ctx, 1 if on else 0))
+
+    def launch_shape(self, n):
+        """The shape a launch of n pixels would use now."""
+        s = abi.LaunchShape()
+        self._check(self._lib.foort_gpu_launch_shape(self._ctx, n, C.byref(s)))
+        return s.as_dict()
+
     def positions(self, px, first):
         """GeodesicPosition of the pixels whose first-pass results are `first`
         (foort_gpu_positions). Returns (counts, points): points is (total, 4)."""
@@ -218,6 +249,47 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+def tune_key(desc, num_sms, n):
+    """The launch-shape cache key of a launch of n pixels (foort_tune_key)."""
+    buf = C.create_string_buffer(160)
+    rc = load().foort_tune_key(C.byref(desc), num_sms, n, buf, len(buf))
+    if rc != 0:
+        raise FoortError(rc, "tune key")
+    return buf.value.decode()
+
+
+def tune_get(key):
+    s = abi.LaunchShape()
+    return s.as_dict() if load().foort_tune_get(key.encode(), C.byref(s)) == 0 else None
+
+
+def tune_put(key, **shape):
+    s = abi.LaunchShape(**shape)
+    rc = load().foort_tune_put(key.encode(), C.byref(s))
+    if rc != 0:
+        raise FoortError(rc, "invalid launch shape or key")
+
+
+def tune_save(path):
+    rc = load().foort_tune_save(os.fsencode(path))
+    if rc != 0:
+        raise FoortError(rc, f"cannot write {path}")
+
+
+def tune_load(path):
+    rc = load().foort_tune_load(os.fsencode(path))
+    if rc != 0:
+        raise FoortError(rc, f"cannot read {path}")
+
+
+def tune_clear():
+    load().foort_tune_clear()
+
+
+def tune_count():
+    return load().foort_tune_count()
 
 
 def horizon_radius(metric_id, params):

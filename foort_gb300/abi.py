@@ -29,6 +29,7 @@ INTEGRATOR_VERLET = 1
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_FP64_ANALYTIC = 2  # every step in FP64 with the mixed kernel's analytic derivatives
 
 MIXED_FP64_DECISIONS = 0x1
 MIXED_FP64_NEAR_HORIZON = 0x2
@@ -147,7 +148,26 @@ class Stats(C.Structure):
         ("n_blocks", C.c_uint32),
         ("block_size", C.c_uint32),
         ("lanes_per_geodesic", C.c_uint32),
+        ("refill_steps", C.c_uint32),
+        ("poll_steps", C.c_uint32),
     ]
+
+
+class LaunchShape(C.Structure):
+    """foort_launch_shape: CTA size, CTA cap per SM, lanes per geodesic, regrouping
+    cadence, poll interval, and the autotuner's measured time."""
+    _fields_ = [
+        ("block_size", C.c_uint32),
+        ("blocks_per_sm", C.c_uint32),
+        ("lanes", C.c_uint32),
+        ("refill_steps", C.c_uint32),
+        ("poll_steps", C.c_uint32),
+        ("reserved", C.c_uint32),
+        ("ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 CONFIG_MESH_SIMPLE = 0

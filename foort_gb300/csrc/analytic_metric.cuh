@@ -27,9 +27,10 @@ struct G5T {
 // squares r0's relative error (~2^-23) away and leaves the final FMA's rounding: within
 // one ulp, in three instructions and without the branches of a correctly rounded
 // reciprocal (which sit on the critical path of every right-hand side). For x = 0 it
-// gives NaN where 1/x is infinite: the factors are r - r_+, r - r_-, sin(theta), Sigma,
-// r and the like, exactly 0 only on a horizon, a pole or the origin, where the state
-// turns non-finite with either value. Passing the infinity through cost C2 1.2 % on
+// gives NaN where 1/x is infinite, and so for any |x| below FLT_MIN, which the .ftz
+// forms flush to 0: the factors are r - r_+, r - r_-, sin(theta), Sigma, r and the like,
+// below 1.2e-38 only within that distance of a horizon, a pole or the origin, where the
+// state turns non-finite with either value. Passing the infinity through cost C2 1.2 % on
 // GB300.
 FOORT_HD float rcp(float x) {
 #ifdef __CUDA_ARCH__
@@ -237,14 +238,15 @@ FOORT_HD void mn_eval(const T* q, double rd, double dpd, double sd, double cd, T
 
 // The largest of |2 alpha3 (1 - (x - y) S1)|, |2 alpha3 (-1 + (x + y) S2)|, |2 psi| and
 // |2 gamma'| (the arguments of Manko-Novikov's exponentials, mn_eval) over theta at
-// radius r, in FP64 (host). FP32 carries an exponent with absolute error ~6e-8 times its
-// size, which becomes the relative error of the metric; near the horizon the exponents
-// grow without bound and the metric leaves FP32's range.
-inline double mn_max_exponent(const MetricConst& M, double r) {
+// radius r (n_theta - 1 interior angles, evenly spaced), in FP64 (host). FP32 carries an
+// exponent with absolute error ~6e-8 times its size, which becomes the relative error of
+// the metric; near the horizon the exponents grow without bound and the metric leaves
+// FP32's range.
+inline double mn_max_exponent(const MetricConst& M, double r, int n_theta = 180) {
     const double a3 = M.q[1], k = M.q[3];
     double worst = 0.0;
-    for (int i = 1; i < 180; ++i) {
-        const double th = 3.14159265358979323846 * i / 180.0, y = std::cos(th), s = std::sin(th);
+    for (int i = 1; i < n_theta; ++i) {
+        const double th = 3.14159265358979323846 * i / n_theta, y = std::cos(th), s = std::sin(th);
         const double x = (r - 1.0) / k, x2m1 = (x - 1.0) * (x + 1.0);
         const double R = std::sqrt(x2m1 + y * y), iR = 1.0 / R, t = x * y * iR, t2 = t * t;
         const double P1 = t, P2 = 0.5 * (3 * t2 - 1), P3 = 0.5 * t * (5 * t2 - 3), P4 = 0.125 * (35 * t2 * t2 - 30 * t2 + 3);

@@ -40,6 +40,7 @@ struct foort_ctx {
     uint32_t lanes = 0;  // lanes per geodesic: 0 chosen per launch, 1, 2
     int device = 0, num_sms = 0;
     bool pending = false;
+    bool autotune = false;  // search shapes for launches without a cache entry
     foort_stats stats{};
     std::string err;
 };
@@ -141,7 +142,10 @@ int validate(const foort_run_desc* d, std::string& why) {
         why = "unknown integrator_id";
         return FOORT_E_BADARG;
     }
-    if (d->precision != FOORT_PREC_FP64 && d->precision != FOORT_PREC_MIXED) { why = "unknown precision"; return FOORT_E_BADARG; }
+    if (d->precision != FOORT_PREC_FP64 && d->precision != FOORT_PREC_MIXED && d->precision != FOORT_PREC_FP64_ANALYTIC) {
+        why = "unknown precision";
+        return FOORT_E_BADARG;
+    }
     if (d->n_images == 0 || !d->images) { why = "no images"; return FOORT_E_BADARG; }
     if (d->term_flags == 0) { why = "no terminations turned on"; return FOORT_E_BADARG; }
     if (d->term_flags & ~0xFu) { why = "unknown termination flag"; return FOORT_E_BADARG; }
@@ -185,7 +189,8 @@ RunConst make_run_const(const foort_run_desc& d) {
     R.cr_start = d.closest_freq.at_start;
     R.cr_finish = d.closest_freq.at_finish;
     R.verlet_cap = 1000;
-    R.poll_steps = 512;
+    R.poll_steps = kDefaultPollSteps;
+    R.refill_steps = 1;
     R.mixed_options = d.mixed_options;
     R.mixed_fp64_margin = (d.mixed_options & FOORT_MIXED_FP64_NEAR_HORIZON) ? d.mixed_fp64_margin : 0.0;
     R.gp_every = d.geopos_freq.every_n;
@@ -194,14 +199,18 @@ RunConst make_run_const(const foort_run_desc& d) {
     return R;
 }
 
+// The analytic-derivative kernels serve FOORT_PREC_MIXED and FOORT_PREC_FP64_ANALYTIC
+// (the latter takes every step in FP64).
+bool analytic_family(int precision) { return precision == FOORT_PREC_MIXED || precision == FOORT_PREC_FP64_ANALYTIC; }
+
 const void* select_kernel(const RunConst& R) {
-    if (R.precision == FOORT_PREC_MIXED)
+    if (analytic_family(R.precision))
         return mixed_kernel_variant(R.metric_id, R.integrator, (R.mixed_options & FOORT_MIXED_FP64_DECISIONS) != 0);
     return fp64_kernel(R.metric_id, R.integrator);
 }
 
-// The two-lanes-per-geodesic kernel for these options, or nullptr (FP64, Verlet, the
-// called plugins, the FP64 right-hand side near the horizon).
+// The two-lanes-per-geodesic kernel for these options, or nullptr (FP64, FP64-analytic,
+// Verlet, the called plugins, the strong-field FP64 steps).
 const void* select_pair_kernel(const RunConst& R) {
     if (R.precision != FOORT_PREC_MIXED || R.mixed_fp64_margin > 0.0) return nullptr;
     return mixed_pair_kernel_variant(R.metric_id, R.integrator, (R.mixed_options & FOORT_MIXED_FP64_DECISIONS) != 0);
@@ -209,32 +218,32 @@ const void* select_pair_kernel(const RunConst& R) {
 
 struct LaunchShape {
     const void* fn = nullptr;
-    uint32_t grid = 0, block = 0, lanes = 1;
+    uint32_t grid = 0, block = 0, lanes = 1, refill = 1, poll = kDefaultPollSteps;
 };
 
-// Kernel and grid of a launch of n geodesics: a persistent grid of at most the resident
-// CTAs. lanes_pref 0 chooses two lanes per geodesic where that kernel exists and all n
-// geodesics fit on the GPU's resident lanes that way (then a step's latency, not the
-// GPU's throughput, sets the pace, and two lanes halve the metric work on it); 1 and 2
-// force one or two lanes where possible.
-int choose_launch(foort_ctx* ctx, const RunConst& R, uint64_t n, int num_sms, uint32_t block_size,
-                  uint32_t blocks_per_sm, uint32_t lanes_pref, LaunchShape& out) {
-    const uint32_t bs = block_size ? block_size : 128;
+// Kernel and grid of a launch of n geodesics in the requested shape (zero fields: the
+// built-in rule): a persistent grid of at most the resident CTAs. The rule takes 128
+// threads, as many CTAs per SM as fit, and two lanes per geodesic where that kernel exists
+// and all n geodesics fit on the GPU's resident lanes that way (then a step's latency,
+// not the GPU's throughput, sets the pace, and two lanes halve the metric work on it).
+int choose_launch(foort_ctx* ctx, const RunConst& R, uint64_t n, int num_sms, const foort_launch_shape& want,
+                  LaunchShape& out) {
+    const uint32_t bs = want.block_size ? want.block_size : 128;
     auto resident = [&](const void* fn, int& per_sm) -> int {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, static_cast<int>(bs), 0));
-        if (blocks_per_sm) per_sm = std::min<int>(per_sm, static_cast<int>(blocks_per_sm));
+        if (want.blocks_per_sm) per_sm = std::min<int>(per_sm, static_cast<int>(want.blocks_per_sm));
         return FOORT_OK;
     };
     const void* fn = select_kernel(R);
     if (!fn) return fail(ctx, FOORT_E_UNSUPPORTED, "no kernel for this metric / integrator / precision");
     int per_sm = 0, rc = 0;
     uint32_t lanes = 1;
-    const void* fn2 = (lanes_pref != 1) ? select_pair_kernel(R) : nullptr;
+    const void* fn2 = (want.lanes != 1) ? select_pair_kernel(R) : nullptr;
     if (fn2) {
         int per_sm2 = 0;
         if ((rc = resident(fn2, per_sm2))) return rc;
         const uint64_t cap2 = static_cast<uint64_t>(per_sm2) * static_cast<uint64_t>(num_sms) * bs;
-        if (per_sm2 > 0 && (lanes_pref == 2 || 2 * n <= cap2)) {
+        if (per_sm2 > 0 && (want.lanes == 2 || 2 * n <= cap2)) {
             fn = fn2;
             per_sm = per_sm2;
             lanes = 2;
@@ -248,7 +257,24 @@ int choose_launch(foort_ctx* ctx, const RunConst& R, uint64_t n, int num_sms, ui
     out.grid = static_cast<uint32_t>(std::max<uint64_t>(1, std::min(full, need)));
     out.block = bs;
     out.lanes = lanes;
+    out.refill = want.refill_steps ? want.refill_steps : 1;
+    out.poll = want.poll_steps ? want.poll_steps : kDefaultPollSteps;
     return FOORT_OK;
+}
+
+// The shape a launch of n geodesics asks for: the cached tuned shape for the context's
+// key, with the context's forced settings (foort_gpu_set_launch / _set_lanes) over it.
+foort_launch_shape requested_shape(const foort_ctx* ctx, uint64_t n, bool* cached = nullptr) {
+    foort_launch_shape s{};
+    char key[160];
+    const bool hit = foort_tune_key(&ctx->desc, ctx->num_sms, n, key, sizeof(key)) == FOORT_OK &&
+                     foort_tune_get(key, &s) == FOORT_OK;
+    if (!hit) s = foort_launch_shape{};
+    if (cached) *cached = hit;
+    if (ctx->block_size) s.block_size = ctx->block_size;
+    if (ctx->blocks_per_sm) s.blocks_per_sm = ctx->blocks_per_sm;
+    if (ctx->lanes) s.lanes = ctx->lanes;
+    return s;
 }
 
 int ensure_capacity(foort_ctx* ctx, uint64_t n) {
@@ -264,10 +290,18 @@ int ensure_capacity(foort_ctx* ctx, uint64_t n) {
     return FOORT_OK;
 }
 
+int autotune_launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, cudaStream_t st,
+                    foort_launch_shape* best);
+
+// One launch over n pixels: the explicit shape if given, else the requested one (with
+// the search first where autotuning is on and the cache has no entry).
 int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, cudaStream_t st,
-           GeoposRec* gp_plan = nullptr) {
+           GeoposRec* gp_plan = nullptr, const foort_launch_shape* shape = nullptr) {
+    bool cached = false;
+    const foort_launch_shape want = shape ? *shape : requested_shape(ctx, n, &cached);
+    if (!shape && !cached && ctx->autotune && !gp_plan && n > 0) return autotune_launch(ctx, d_px, n, d_out, st, nullptr);
     LaunchShape ls;
-    int rc = choose_launch(ctx, ctx->rc, n, ctx->num_sms, ctx->block_size, ctx->blocks_per_sm, ctx->lanes, ls);
+    int rc = choose_launch(ctx, ctx->rc, n, ctx->num_sms, want, ls);
     if (rc) return rc;
     const void* fn = ls.fn;
     const uint32_t bs = ls.block, grid = ls.grid;
@@ -289,6 +323,8 @@ int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_
         A.budget = std::max<unsigned long long>(100000000ull, 1000000ull * n);
     }
     RunConst R = ctx->rc;
+    R.refill_steps = static_cast<int32_t>(ls.refill);
+    R.poll_steps = static_cast<int32_t>(ls.poll);
     void* args[2] = {&A, &R};
     CK(cudaEventRecord(ctx->ev0, st));
     if (n > 0) CK(cudaLaunchKernel(fn, dim3(grid), dim3(bs), args, 0, st));
@@ -297,6 +333,8 @@ int launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_
     ctx->stats.n_blocks = grid;
     ctx->stats.block_size = bs;
     ctx->stats.lanes_per_geodesic = ls.lanes;
+    ctx->stats.refill_steps = ls.refill;
+    ctx->stats.poll_steps = ls.poll;
     ctx->last_n = n;
     ctx->last_stream = st;
     ctx->pending = true;
@@ -342,6 +380,85 @@ int finish(foort_ctx* ctx) {
     else if (st & kStatusBudget) rc = fail(ctx, FOORT_E_BUDGET, "global step budget exhausted; unfinished geodesics are marked");
     ctx->stats.status = static_cast<uint32_t>(rc);
     return rc;
+}
+
+// The search (foort_gpu_autotune). Candidates: lanes per geodesic (1, and 2 where the
+// two-lane kernel exists) times CTA sizes 32, 64, 128, at refill cadence 1 and the default
+// poll interval; then, around the fastest, refill cadences 4 and 16 and poll intervals
+// 128 and 2048; the two fastest are timed once more and the smaller time counts. Each
+// candidate is one launch over the pixels (or a prefix, for launches much larger than the
+// GPU's resident lanes), timed with CUDA events. The last launch integrates all n pixels
+// in the winning shape.
+int autotune_launch(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, cudaStream_t st,
+                    foort_launch_shape* best_out) {
+    LaunchShape probe;
+    int rc = choose_launch(ctx, ctx->rc, 1, ctx->num_sms, foort_launch_shape{128, 0, 1, 1, kDefaultPollSteps, 0, 0.0},
+                           probe);
+    if (rc) return rc;
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, probe.fn, 128, 0));
+    const uint64_t resident = static_cast<uint64_t>(std::max(per_sm, 1)) * ctx->num_sms * 128;
+    const uint64_t m = std::min<uint64_t>(n, FOORT_TUNE_SAMPLE_LANES_X * resident);
+    const bool has_pair = select_pair_kernel(ctx->rc) != nullptr;
+    std::vector<foort_launch_shape> tried;
+    auto time_shape = [&](foort_launch_shape s, double& ms) -> int {
+        int r = launch(ctx, d_px, m, d_out, st, nullptr, &s);
+        if (r) return r;
+        r = finish(ctx);
+        if (r != FOORT_OK) return r;
+        ms = ctx->stats.kernel_ms;
+        return FOORT_OK;
+    };
+    auto consider = [&](foort_launch_shape s) -> int {
+        for (const auto& t : tried)
+            if (t.block_size == s.block_size && t.lanes == s.lanes && t.refill_steps == s.refill_steps &&
+                t.poll_steps == s.poll_steps && t.blocks_per_sm == s.blocks_per_sm)
+                return FOORT_OK;
+        double ms = 0.0;
+        int r = time_shape(s, ms);
+        if (r) return r;
+        s.ms = ms;
+        tried.push_back(s);
+        return FOORT_OK;
+    };
+    auto fastest = [&]() {
+        size_t b = 0;
+        for (size_t i = 1; i < tried.size(); ++i)
+            if (tried[i].ms < tried[b].ms) b = i;
+        return tried[b];
+    };
+    // one untimed launch: module load and first-touch costs stay out of the comparison
+    double warm = 0.0;
+    if ((rc = time_shape(foort_launch_shape{128, 0, 1, 1, kDefaultPollSteps, 0, 0.0}, warm))) return rc;
+    for (uint32_t lanes = 1; lanes <= (has_pair ? 2u : 1u); ++lanes)
+        for (uint32_t bs : {32u, 64u, 128u})
+            if ((rc = consider(foort_launch_shape{bs, 0, lanes, 1, kDefaultPollSteps, 0, 0.0}))) return rc;
+    foort_launch_shape b = fastest();
+    for (uint32_t refill : {4u, 16u}) {
+        foort_launch_shape c = b;
+        c.refill_steps = refill;
+        if ((rc = consider(c))) return rc;
+    }
+    b = fastest();
+    for (uint32_t poll : {128u, 2048u}) {
+        foort_launch_shape c = b;
+        c.poll_steps = poll;
+        if ((rc = consider(c))) return rc;
+    }
+    // the two fastest once more
+    std::sort(tried.begin(), tried.end(),
+              [](const foort_launch_shape& x, const foort_launch_shape& y) { return x.ms < y.ms; });
+    for (size_t i = 0; i < std::min<size_t>(2, tried.size()); ++i) {
+        double ms = 0.0;
+        if ((rc = time_shape(tried[i], ms))) return rc;
+        tried[i].ms = std::min(tried[i].ms, ms);
+    }
+    b = fastest();
+    char key[160];
+    if (foort_tune_key(&ctx->desc, ctx->num_sms, n, key, sizeof(key)) == FOORT_OK) foort_tune_put(key, &b);
+    if (best_out) *best_out = b;
+    // the real launch: every pixel, the winning shape
+    return launch(ctx, d_px, n, d_out, st, nullptr, &b);
 }
 
 }  // namespace
@@ -393,7 +510,7 @@ int foort_gpu_create(const foort_run_desc* desc, foort_ctx** out_ctx) {
         ic.m = make_metric_const(desc->metric_id, desc->images[i].metric_params);
         camera_frame(desc->metric_id, ctx->rc.rlog != 0, desc->images[i], ic);
         ic.h_eps = desc->images[i].horizon_eps > 0.0 ? desc->images[i].horizon_eps : desc->horizon_eps;
-        if (ctx->rc.precision == FOORT_PREC_MIXED) fill_mixed_constants(desc->metric_id, ic, ctx->rc);
+        if (analytic_family(ctx->rc.precision)) fill_mixed_constants(desc->metric_id, ic, ctx->rc);
     }
     auto bail = [&](int rc) {
         std::string m = ctx->err;
@@ -546,6 +663,33 @@ int foort_gpu_set_lanes(foort_ctx* ctx, uint32_t lanes_per_geodesic) {
     return FOORT_OK;
 }
 
+int foort_gpu_autotune(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out, void* cuda_stream,
+                       foort_launch_shape* best) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    if (n == 0 || !d_px || !d_out) return fail(ctx, FOORT_E_BADARG, "autotuning needs pixels and a result buffer");
+    int rc = finish(ctx);
+    if (rc != FOORT_OK && rc != FOORT_E_BUDGET && rc != FOORT_E_CANCELLED) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    if ((rc = autotune_launch(ctx, d_px, n, d_out, st, best))) return rc;
+    return finish(ctx);
+}
+
+int foort_gpu_set_autotune(foort_ctx* ctx, int32_t on) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    ctx->autotune = on != 0;
+    return FOORT_OK;
+}
+
+int foort_gpu_launch_shape(foort_ctx* ctx, uint64_t n, foort_launch_shape* shape) {
+    if (!ctx || !shape) return fail(ctx, FOORT_E_BADARG, "NULL argument");
+    const foort_launch_shape want = requested_shape(ctx, n);
+    LaunchShape ls;
+    const int rc = choose_launch(ctx, ctx->rc, n, ctx->num_sms, want, ls);
+    if (rc) return rc;
+    *shape = foort_launch_shape{ls.block, want.blocks_per_sm, ls.lanes, ls.refill, ls.poll, 0, want.ms};
+    return FOORT_OK;
+}
+
 int foort_gpu_get_desc(const foort_ctx* ctx, foort_run_desc* desc) {
     if (!ctx || !desc) return FOORT_E_BADARG;
     *desc = ctx->desc;  // images: the context's own copy
@@ -587,7 +731,7 @@ int foort_gpu_has_kernel(int32_t metric_id, int32_t integrator_id, int32_t preci
     if (metric_id < 0 || metric_id > 4) return 0;
     if (integrator_id != FOORT_INTEGRATOR_RK4 && integrator_id != FOORT_INTEGRATOR_VERLET) return 0;
     if (precision == FOORT_PREC_FP64) return fp64_kernel(metric_id, integrator_id) != nullptr;
-    if (precision == FOORT_PREC_MIXED) return mixed_kernel(metric_id, integrator_id) != nullptr;
+    if (analytic_family(precision)) return mixed_kernel(metric_id, integrator_id) != nullptr;
     return 0;
 }
 
@@ -711,13 +855,13 @@ extern "C" int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foo
         ic.m = make_metric_const(desc->metric_id, desc->images[i].metric_params);
         camera_frame(desc->metric_id, R0.rlog != 0, desc->images[i], ic);
         ic.h_eps = desc->images[i].horizon_eps > 0.0 ? desc->images[i].horizon_eps : desc->horizon_eps;
-        if (R0.precision == FOORT_PREC_MIXED) fill_mixed_constants(desc->metric_id, ic, R0);
+        if (analytic_family(R0.precision)) fill_mixed_constants(desc->metric_id, ic, R0);
         CK(cudaMemcpyAsync(d_images + i, &ic, sizeof(ic), cudaMemcpyHostToDevice, st));
     }
     CK(cudaMemsetAsync(d_ctr, 0, kNumCtr * sizeof(unsigned long long), st));
 
     LaunchShape ls;
-    if ((rc = choose_launch(nullptr, R0, n, nd.num_sms, 0, 0, 0, ls))) return rc;
+    if ((rc = choose_launch(nullptr, R0, n, nd.num_sms, foort_launch_shape{}, ls))) return rc;
     const uint32_t bs = ls.block, grid = ls.grid;
     fn = ls.fn;
     LaunchArgs A{};
@@ -731,6 +875,8 @@ extern "C" int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foo
     A.budget = 0;
     if (!(R0.term_flags & FOORT_TERM_TIMEOUT)) A.budget = std::max<unsigned long long>(100000000ull, 1000000ull * n);
     RunConst R = R0;
+    R.refill_steps = static_cast<int32_t>(ls.refill);
+    R.poll_steps = static_cast<int32_t>(ls.poll);
     void* args[2] = {&A, &R};
     if (n > 0) CK(cudaLaunchKernel(fn, dim3(grid), dim3(bs), args, 0, st));
     if (!stats) return FOORT_OK;
@@ -746,6 +892,8 @@ extern "C" int foort_gpu_integrate_noalloc(const foort_run_desc* desc, const foo
     stats->n_blocks = grid;
     stats->block_size = bs;
     stats->lanes_per_geodesic = ls.lanes;
+    stats->refill_steps = ls.refill;
+    stats->poll_steps = ls.poll;
     rc = FOORT_OK;
     if (h_ctr[kCtrStatus] & kStatusBudget)
         rc = fail(nullptr, FOORT_E_BUDGET, "global step budget exhausted; unfinished geodesics are marked");

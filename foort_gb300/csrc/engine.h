@@ -72,7 +72,7 @@ struct RunConst {
     int32_t verlet_cap;   // cap on Verlet velocity iterations (the reference has none)
     int32_t poll_steps;   // steps between budget / cancel polls
     uint32_t mixed_options;
-    uint32_t pad0;
+    int32_t refill_steps;  // steps a warp runs between refills of its idle lanes (>= 1)
     double mixed_fp64_margin;
     uint64_t gp_every;  // GeodesicPosition update frequency (recorded on a second pass)
     int32_t gp_start, gp_finish;
@@ -88,6 +88,9 @@ enum Ctr {
     kCtrStatus = 5,    // FOORT_STATUS_* bits
     kNumCtr = 8
 };
+
+// Steps between budget / cancel polls unless a launch shape says otherwise.
+constexpr uint32_t kDefaultPollSteps = 512;
 
 // Status bits written by the kernel.
 constexpr unsigned long long kStatusBudget = 1ull;

@@ -173,6 +173,17 @@ __device__ __forceinline__ void reset_lane_state(const RunConst& R, const double
     T.tcur = 0;
 }
 
+// ---- step size ------------------------------------------------------------------------
+// Integrators::GetAdaptiveStep, Integrators.cpp:34-46
+__device__ __forceinline__ double adaptive_step_fp64(const RunConst& R, const double x[4], const double v[4]) {
+    double d1 = R.eps / (fabs(v[1]) + 1e-20);
+    double m = (kRefPi - x[2] < x[2]) ? kRefPi - x[2] : x[2];
+    double d2 = R.eps * m / (fabs(v[2]) + 1e-20);
+    double d3 = R.eps / fabs(v[3] + 1e-20);
+    double h = 1 / (1 / fabs(d1) + 1 / fabs(d2) + 1 / fabs(d3));
+    return (h < R.hmin) ? R.hmin : h;
+}
+
 // ---- initial conditions (ViewScreen.cpp:75-119) ----------------------------------------
 __device__ __forceinline__ void initial_conditions(const ImageConst& I, const foort_pixel& p, double x[4], double v[4]) {
     for (int i = 0; i < 4; ++i) x[i] = I.pos0[i];
@@ -239,9 +250,12 @@ __device__ __forceinline__ bool finite4(const double a[4]) {
 //   counters: L.rhs, L.fp64            accumulated per lane, flushed at each poll
 //
 // Every warp takes pixels from one global counter (one atomic per warp, shared by the
-// lanes that need work) and keeps integrating until the queue is empty. A lane whose
-// geodesic terminates takes the next pixel at once, so lanes of a warp stay busy while
-// geodesics of very different lengths run side by side. Every R.poll_steps iterations a
+// lanes that need work) and keeps integrating until the queue is empty. Lanes whose
+// geodesics terminated take the next pixels at the warp's next refill, at most
+// R.refill_steps steps later (the regrouping cadence; 1 = at once), so lanes of a warp
+// stay busy while geodesics of very different lengths run side by side; a longer cadence
+// refills several lanes with one atomic and one pass of the initial conditions. Every
+// R.poll_steps iterations a
 // warp publishes its step count, checks the step budget and the host cancel flag, and
 // learns whether another warp has asked every lane to stop. No loop waits on another
 // thread or on the host.
@@ -264,10 +278,11 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
     uint32_t stop_err = 0;
     uint64_t idx = 0;
     unsigned long long lane_steps = 0, lane_done = 0;
-    int since_poll = 0;
+    int since_poll = 0, since_refill = 0;
 
     for (;;) {
         // Refill idle lanes from the queue.
+        since_refill = 0;
         if (!drained) {
             const unsigned need = __ballot_sync(kFullMask, !active) & slots;
             if (need) {
@@ -323,10 +338,11 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                 }
             }
             ++since_poll;
+            ++since_refill;
             if (since_poll >= R.poll_steps) break;
             const unsigned idle = __ballot_sync(kFullMask, !active);
             if (idle == kFullMask) break;
-            if (idle && !drained) break;
+            if (idle && !drained && since_refill >= R.refill_steps) break;
         }
         if (since_poll >= R.poll_steps || drained) {
             since_poll = 0;

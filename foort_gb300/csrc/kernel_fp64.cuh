@@ -67,16 +67,6 @@ __device__ __forceinline__ void rhs_fd_fp64(const MetricConst& M, bool rlog, dou
     contract_fp64(fd_parts_fp64<MID>(M, rlog, hfd, x), v, acc);
 }
 
-// Integrators::GetAdaptiveStep, Integrators.cpp:34-46
-__device__ __forceinline__ double adaptive_step_fp64(const RunConst& R, const double x[4], const double v[4]) {
-    double d1 = R.eps / (fabs(v[1]) + 1e-20);
-    double m = (kRefPi - x[2] < x[2]) ? kRefPi - x[2] : x[2];
-    double d2 = R.eps * m / (fabs(v[2]) + 1e-20);
-    double d3 = R.eps / fabs(v[3] + 1e-20);
-    double h = 1 / (1 / fabs(d1) + 1 / fabs(d2) + 1 / fabs(d3));
-    return (h < R.hmin) ? R.hmin : h;
-}
-
 template <int MID, int INTEG>
 struct Fp64Engine {
     struct Lane {

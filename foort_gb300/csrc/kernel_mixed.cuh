@@ -12,8 +12,9 @@
 // Decisions (terminations, equator crossings, closest radius) are taken on the
 // compensated state; with DECIDE64 they are taken in FP64 on its exact double value,
 // as the reference takes them, otherwise by float-float comparisons that agree with
-// the FP64 ones except within 2^-48 (relative) of a threshold. Optionally, lanes closer
-// than I.r_fp64 to the horizon evaluate their right-hand side in FP64.
+// the FP64 ones except within 2^-48 (relative) of a threshold. Optionally, lanes inside
+// the strong-field radius I.r_fp64 take their whole step in FP64 (step_fp64): there the
+// ray bends most, and bending amplifies every error a step makes.
 #pragma once
 
 #include "analytic_metric.cuh"
@@ -65,6 +66,17 @@ __host__ __device__ inline void ff_split(double d, float& hi, float& lo) {
     lo = static_cast<float>(d - static_cast<double>(hi));
 }
 __device__ __forceinline__ ff ff_of(const float* p) { return {p[0], p[1]}; }
+__device__ __forceinline__ ff ff_from_d(double d) {
+    const float hi = __double2float_rn(d);
+    return {hi, __double2float_rn(d - static_cast<double>(hi))};
+}
+// a + (bh + bl) for a small second term bl (|bl| well below |bh|, or bh = 0): bh joins
+// a's high part exactly (TwoSum), bl its low part.
+__device__ __forceinline__ ff ff_add_f2(ff a, float bh, float bl) {
+    ff s = two_sum(a.hi, bh);
+    s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, bl));
+    return fast_two_sum(s.hi, s.lo);
+}
 
 // The right-hand side in two parts: the metric part depends on the position only (the
 // expensive part: angle, metric derivatives, inverse metric), the contraction with the
@@ -125,6 +137,32 @@ __device__ __forceinline__ MetricAt<T> metric_part(const T* q, const MixedConst&
     return m;
 }
 
+// Metric part in FP64 at a double position (the strong-field steps). r - r_+ and r - r_-
+// are formed in FP64 (in log-r mode through expm1 of ln(r / r_+)), so Delta keeps its
+// relative accuracy down to the horizon.
+template <int MID>
+__device__ __forceinline__ MetricAt<double> metric_part_d(const double* q, const MixedConst& mc, bool rlog, double x1,
+                                                          double th) {
+    double r, dp, dm;
+    if (!rlog) {
+        r = x1;
+        dp = x1 - mc.rpv;
+        dm = x1 - mc.rmv;
+    } else {
+        r = exp(x1);
+        const double lrp = double(mc.lrp[0]) + double(mc.lrp[1]);
+        dp = (mc.rpv > 0.0) ? mc.rpv * expm1(x1 - lrp) : r;
+        dm = (mc.rmv > 0.0) ? mc.rmv * expm1(x1 - (double(mc.lrm[0]) + double(mc.lrm[1]))) : r;
+    }
+    double s, c;
+    sincos(th, &s, &c);
+    MetricAt<double> m;
+    double grr;
+    MixedMetric<MID>::template eval<double>(q, r, dp, dm, s, c, m.d1, m.d2, m.gu, grr);
+    if (rlog) scale_log_r(r, m.d1, m.d2, m.gu);
+    return m;
+}
+
 // Contraction with the velocity (accel_lagrange; in log-r mode plus the exact coordinate
 // term -(u^1)^2 of accel_log_r).
 template <typename T>
@@ -161,21 +199,109 @@ __device__ __noinline__ MetricAt<float> metric_part_called(const float* q, const
     return metric_part<MID, float>(q, mc, rlog, x1, th);
 }
 
-template <int MID>
-__device__ __noinline__ void rhs_fp64_path(const double* q, const MixedConst& mc, bool rlog, ff x1, ff th,
-                                           const float uf[4], float a[4]) {
-    double u[4] = {uf[0], uf[1], uf[2], uf[3]}, ad[4];
-    rhs_analytic<MID, double>(q, mc, rlog, x1, th, u, ad);
-    for (int i = 0; i < 4; ++i) a[i] = static_cast<float>(ad[i]);
+// The increments of one step taken wholly in FP64, with its counts.
+struct StepD {
+    double dx[4], dv[4];
+    double h;
+    uint32_t rhs, err;
+};
+
+// One step in FP64 (the strong-field region): the reference's RK4 (Integrators.cpp:51-94)
+// or velocity Verlet (Integrators.cpp:99-152) and its step rule (Integrators.cpp:34-46),
+// with the analytic right-hand side, from the position (x1, theta) and the velocity u
+// as doubles. Everything a step carries -- stage positions and velocities, the
+// accelerations, the increments -- stays in FP64: an FP64 right-hand side fed with
+// velocities rounded to FP32 would keep their 6e-8 relative error, which strongly bent
+// rays amplify as much as the FP32 right-hand side's own.
+template <int MID, int INTEG>
+__device__ __noinline__ StepD step_fp64(const ImageConst& I, const RunConst& R, double x1, double th, double u0,
+                                        double u1, double u2, double u3) {
+    const bool rlog = R.rlog != 0;
+    const double* q = I.qa;
+    const double u[4] = {u0, u1, u2, u3};
+    const double xs[4] = {0.0, x1, th, 0.0};
+    StepD d;
+    d.err = 0;
+    const double h = adaptive_step_fp64(R, xs, u);
+    d.h = h;
+    if (INTEG == FOORT_INTEGRATOR_RK4) {
+        double k1[4], k2[4], k3[4], k4[4], us[4];
+        const double hh = 0.5 * h;
+        accel_part(metric_part_d<MID>(q, I.mx, rlog, x1, th), rlog, u, k1);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = u[i] + hh * k1[i];
+        accel_part(metric_part_d<MID>(q, I.mx, rlog, x1 + hh * u[1], th + hh * u[2]), rlog, us, k2);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = u[i] + hh * k2[i];
+        accel_part(metric_part_d<MID>(q, I.mx, rlog, x1 + hh * (u[1] + hh * k1[1]), th + hh * (u[2] + hh * k1[2])),
+                   rlog, us, k3);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) us[i] = u[i] + h * k3[i];
+        accel_part(metric_part_d<MID>(q, I.mx, rlog, x1 + h * (u[1] + hh * k2[1]), th + h * (u[2] + hh * k2[2])),
+                   rlog, us, k4);
+        const double h6 = h / 6.0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            d.dv[i] = (((k1[i] + k2[i] * 2) + k3[i] * 2) + k4[i]) * h6;
+            d.dx[i] = u[i] * h + ((k1[i] + k2[i]) + k3[i]) * (h * h6);
+        }
+        d.rhs = 4;
+        return d;
+    }
+    double a0[4], a1[4], vi[4];
+    accel_part(metric_part_d<MID>(q, I.mx, rlog, x1, th), rlog, u, a0);
+    const double hh2 = h * h / 2.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        d.dx[i] = u[i] * h + a0[i] * hh2;
+        vi[i] = u[i] + a0[i] * h;
+    }
+    const MetricAt<double> mn = metric_part_d<MID>(q, I.mx, rlog, x1 + d.dx[1], th + d.dx[2]);
+    accel_part(mn, rlog, vi, a1);
+    const double h2 = h / 2.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) d.dv[i] = (a0[i] + a1[i]) * h2;
+    d.rhs = 2;
+    if (R.vtol > 0.0) {
+        const double tol2 = R.vtol * R.vtol;
+        for (int it = 0;; ++it) {
+            double num = 0.0, den = 0.0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const double nv = u[i] + d.dv[i];
+                const double e = nv - vi[i];
+                num += e * e;
+                den += nv * nv;
+            }
+            if (!(num / den > tol2)) break;
+            if (it >= R.verlet_cap) {
+                d.err |= FOORT_ERR_VERLET_ITER;
+                break;
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) vi[i] = u[i] + d.dv[i];
+            accel_part(mn, rlog, vi, a1);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) d.dv[i] = (a0[i] + a1[i]) * h2;
+            d.rhs += 1;
+        }
+    }
+    return d;
 }
 
 // Integrators::GetAdaptiveStep (Integrators.cpp:34-46) in FP32. Written as
 //     h = eps / ((|u1| + d) + (|u2| + d) / m + |u3 + d|),  m = min(theta, pi - theta),
-// which is the reference's expression with eps factored out, evaluated with correctly
-// rounded operations and eps carried as a float-float pair: the step size then has no
-// systematic bias against the FP64 kernel's (a bias would shift where along the ray
-// the last step lands). pi - theta is formed in float-float: near the pole both round to
-// the same float, and a zero m would collapse the step to the smallest step size.
+// which is the reference's expression with eps factored out, with eps carried as a
+// float-float pair: the step size then has no systematic bias against the FP64 kernel's
+// (a bias would shift every ray's affine parameter, and strongly bent rays turn a shift
+// into an error of their end points). The quotient is formed from the reciprocal with its
+// residual: q0 = eps_hi (1/s), then q = q0 + (eps_hi - q0 s + eps_lo) / s. Taking eps_hi
+// times the rounded 1/s instead is biased: far from the hole s = |u^1| + ... lies just
+// below 1, where floats are twice as dense as just above 1, so every other 1/s falls just
+// past a rounding midpoint and rounds up, making h about 3e-8 too large on average; over
+// 10^5 steps that moved C2's end points by 1e-6 on a tenth of its rays. pi - theta is
+// formed in float-float: near the pole both round to the same float, and a zero m would
+// collapse the step to the smallest step size.
 __device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const MixedConst& mc, ff th, const float v[4]) {
     const ff dpi = ff_add(ff_of(mc.pi), ff_neg(th));
     const float t = ff_f(th), pt = ff_f(dpi);
@@ -183,15 +309,19 @@ __device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const Mixe
     const float s1 = __fadd_rn(fabsf(v[1]), 1e-20f);
     const float s2 = __fmul_rn(__fadd_rn(fabsf(v[2]), 1e-20f), rcp(fabsf(m)));
     const float s3 = fabsf(__fadd_rn(v[3], 1e-20f));
-    const float inv = rcp(__fadd_rn(__fadd_rn(s1, s2), s3));
-    const float h = __fmaf_rn(mc.eps[0], inv, __fmul_rn(mc.eps[1], inv));
+    const float sum = __fadd_rn(__fadd_rn(s1, s2), s3);
+    const float inv = rcp(sum);
+    const float q0 = __fmul_rn(mc.eps[0], inv);
+    const float res = __fmaf_rn(-q0, sum, mc.eps[0]);  // eps_hi - q0 s, exact
+    const float h = __fmaf_rn(__fadd_rn(res, mc.eps[1]), inv, q0);
     const float hmin = mc.hmin;
     return (h < hmin) ? hmin : h;
 }
 
 template <int MID, int INTEG, bool DECIDE64>
 struct MixedEngine {
-    // step_pair exists for RK4 with an inlined plugin, without the FP64 near-horizon path
+    // step_pair exists for RK4 with an inlined plugin, without the strong-field FP64 steps
+    // (kept out of it, their call raised the two-lane kernel from 111 to 158 registers)
     static constexpr bool kPairCapable = INTEG == FOORT_INTEGRATOR_RK4 && MixedMetric<MID>::kInline;
 
     struct Lane {
@@ -345,15 +475,11 @@ struct MixedEngine {
         return FOORT_TERMCODE_CONTINUE;
     }
 
-    // A right-hand side through the plugin's FP32 form (inlined or called) or, inside
-    // r_+ + margin when that option is on, the FP64 one; fp64 counts the latter.
-    static __device__ __forceinline__ void rhs(const ImageConst& I, const RunConst& R, uint32_t& fp64, ff x1, ff th,
-                                               const float u[4], float a[4]) {
+    // A right-hand side through the plugin's FP32 form (inlined or called).
+    static __device__ __forceinline__ void rhs(const ImageConst& I, const RunConst& R, ff x1, ff th, const float u[4],
+                                               float a[4]) {
         const bool rlog = R.rlog != 0;
-        if (I.mx.r_fp64 > 0.f && x1.hi < I.mx.r_fp64) {
-            rhs_fp64_path<MID>(I.qa, I.mx, rlog, x1, th, u, a);
-            ++fp64;
-        } else if (MixedMetric<MID>::kInline) {
+        if (MixedMetric<MID>::kInline) {
             rhs_analytic<MID, float>(I.mx.q, I.mx, rlog, x1, th, u, a);
         } else {
             const F4 r = rhs_f32_called<MID>(I.mx.q, I.mx, rlog, x1, th, F4{u[0], u[1], u[2], u[3]});
@@ -364,24 +490,47 @@ struct MixedEngine {
         }
     }
 
-    // One Geodesic::Update (Geodesic.cpp:61-88) through the integrator's step. The
-    // common cases run inline: RK4 with an inlined plugin (stages reordered) and Verlet
-    // with its kept metric part. Everything that evaluates right-hand sides through rhs()
-    // -- RK4 with a called plugin, and the FP64 right-hand side near the horizon -- runs
-    // in step_general, out of line: kept in the kernel, its calls' register needs made
-    // the C4 (Johannsen, Verlet) kernel 22 % slower on GB300 although it never ran them.
+    // Whether this step is taken in FP64: lanes inside the strong-field radius r_fp64
+    // (ln r in log-r mode; 0 = never), decided on the step's starting position.
+    static __device__ __forceinline__ bool in_fp64_region(const ImageConst& I, const Lane& L) {
+        return I.mx.r_fp64 > 0.f && L.x[1].hi < I.mx.r_fp64;
+    }
+
+    // A step in FP64 (step_fp64) applied to the compensated state. `count`: this lane
+    // counts the step's right-hand sides (both lanes of a pair take the same step).
+    static __device__ __forceinline__ bool step_d(Lane& L, const ImageConst& I, const RunConst& R, bool count) {
+        const StepD d = step_fp64<MID, INTEG>(I, R, ff_d(L.x[1]), ff_d(L.x[2]), ff_d(L.v[0]), ff_d(L.v[1]),
+                                              ff_d(L.v[2]), ff_d(L.v[3]));
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            L.x[i] = ff_from_d(ff_d(L.x[i]) + d.dx[i]);
+            L.v[i] = ff_from_d(ff_d(L.v[i]) + d.dv[i]);
+        }
+        if (count) {
+            L.rhs += d.rhs;
+            ++L.fp64;
+        }
+        L.err |= d.err;
+        return after_step(L, I, R, ff_add(L.lam, ff_from_d(d.h)));
+    }
+
+    // One Geodesic::Update (Geodesic.cpp:61-88) through the integrator's step. Inside the
+    // strong-field radius the whole step runs in FP64 (step_d). Otherwise the common cases
+    // run inline: RK4 with an inlined plugin (stages reordered) and Verlet with its kept
+    // metric part. Everything that evaluates right-hand sides through rhs() -- RK4 with a
+    // called plugin, Verlet where the strong-field radius is set -- runs in step_general,
+    // out of line: kept in the kernel, its calls' register needs made the C4 (Johannsen,
+    // Verlet) kernel 22 % slower on GB300 although it never ran them.
     static __device__ __forceinline__ bool step(Lane& L, const ImageConst& I, const RunConst& R) {
+        if (in_fp64_region(I, L)) return step_d(L, I, R, true);
         float uf[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) uf[i] = ff_f(L.v[i]);
         const float h = adaptive_step_f32(R, I.mx, L.x[2], uf);
-        if (!(I.mx.r_fp64 > 0.f)) {
-            if (INTEG == FOORT_INTEGRATOR_VERLET) return step_verlet_cached(L, I, R, h, uf);
-            if (MixedMetric<MID>::kInline) return step_rk4_inline(L, I, R, h, uf);
-        }
+        if (INTEG == FOORT_INTEGRATOR_VERLET && verlet_cached(I)) return step_verlet_cached(L, I, R, h, uf);
+        if (INTEG == FOORT_INTEGRATOR_RK4 && MixedMetric<MID>::kInline) return step_rk4_inline(L, I, R, h, uf);
         const Incr d = step_general(I, R, L.x[1], L.x[2], L.v[1], L.v[2], F4{uf[0], uf[1], uf[2], uf[3]}, h);
         L.rhs += d.rhs;
-        L.fp64 += d.fp64;
         L.err |= d.err;
         return advance(L, I, R, h, d.du, d.dxc);
     }
@@ -422,7 +571,7 @@ struct MixedEngine {
     // The increments of one step taken by step_general, with its counts.
     struct Incr {
         float du[4], dxc[4];
-        uint32_t rhs, fp64, err;
+        uint32_t rhs, err;
     };
 
     // RK4 (Integrators.cpp:51-94) and velocity Verlet (Integrators.cpp:99-152) through
@@ -431,28 +580,27 @@ struct MixedEngine {
     static __device__ __noinline__ Incr step_general(const ImageConst& I, const RunConst& R, ff x1, ff th, ff v1, ff v2,
                                                      F4 u4, float h) {
         Incr d;
-        d.fp64 = 0;
         d.err = 0;
         const float uf[4] = {u4.x, u4.y, u4.z, u4.w};
         if (INTEG == FOORT_INTEGRATOR_RK4) {
             float k1[4], k2[4], k3[4], k4[4], us[4];
             const float hh = 0.5f * h;
-            rhs(I, R, d.fp64, x1, th, uf, k1);
+            rhs(I, R, x1, th, uf, k1);
 #pragma unroll
             for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k1[i];
-            rhs(I, R, d.fp64, ff_add_f(x1, hh * uf[1]), ff_add_f(th, hh * uf[2]), us, k2);
+            rhs(I, R, ff_add_f(x1, hh * uf[1]), ff_add_f(th, hh * uf[2]), us, k2);
 #pragma unroll
             for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
-            rhs(I, R, d.fp64, ff_add_f(x1, hh * (uf[1] + hh * k1[1])), ff_add_f(th, hh * (uf[2] + hh * k1[2])), us, k3);
+            rhs(I, R, ff_add_f(x1, hh * (uf[1] + hh * k1[1])), ff_add_f(th, hh * (uf[2] + hh * k1[2])), us, k3);
 #pragma unroll
             for (int i = 0; i < 4; ++i) us[i] = uf[i] + h * k3[i];
-            rhs(I, R, d.fp64, ff_add_f(x1, h * (uf[1] + hh * k2[1])), ff_add_f(th, h * (uf[2] + hh * k2[2])), us, k4);
+            rhs(I, R, ff_add_f(x1, h * (uf[1] + hh * k2[1])), ff_add_f(th, h * (uf[2] + hh * k2[2])), us, k4);
             rk4_combine(h, k1, k2, k3, k4, d.du, d.dxc);
             d.rhs = 4;
             return d;
         }
         float a0[4], a1[4], vi[4];
-        rhs(I, R, d.fp64, x1, th, uf, a0);
+        rhs(I, R, x1, th, uf, a0);
         const float hh2 = 0.5f * h * h;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -461,7 +609,7 @@ struct MixedEngine {
         }
         const ff x1n = ff_add_f(ff_add(x1, two_prod(h, v1.hi)), __fmaf_rn(h, v1.lo, d.dxc[1]));
         const ff thn = ff_add_f(ff_add(th, two_prod(h, v2.hi)), __fmaf_rn(h, v2.lo, d.dxc[2]));
-        rhs(I, R, d.fp64, x1n, thn, vi, a1);
+        rhs(I, R, x1n, thn, vi, a1);
         d.rhs = 2;
         const float h2 = 0.5f * h;
 #pragma unroll
@@ -487,7 +635,7 @@ struct MixedEngine {
                 float a1n[4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) vi[i] = uf[i] + d.du[i];
-                rhs(I, R, d.fp64, x1n, thn, vi, a1n);
+                rhs(I, R, x1n, thn, vi, a1n);
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
                     dv[i] = h2 * (a1n[i] - a1[i]);
@@ -634,20 +782,30 @@ struct MixedEngine {
     static __device__ __forceinline__ bool advance(Lane& L, const ImageConst& I, const RunConst& R, float h,
                                                    const float du[4], const float dxc[4], const ff* x1n = nullptr,
                                                    const ff* thn = nullptr) {
-        // The increments are rounded to one float each (relative error 6e-8 of a step's
-        // change, unbiased, so it accumulates as a random walk); what the float-float sum
-        // prevents is the absorption of small increments into the large coordinate.
-        // x1n / thn: the new x1 and theta where the caller already formed them.
+        // h u is formed from the whole float-float velocity: its high part h u.hi exactly
+        // (TwoProd) and joined to the position exactly (TwoSum); h u.lo, the product's
+        // rounding error and the O(h^2) part dxc go to the low part. Rounding h u to one
+        // float instead, or dropping u.lo, would put 6e-8 of relative error on every
+        // position increment, which strongly bent rays amplify. du and dxc themselves
+        // carry the FP32 right-hand side's error. x1n / thn: the new x1 and theta where
+        // the caller already formed them.
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            L.x[i] = ff_add_f(L.x[i], __fmaf_rn(h, L.v[i].hi, dxc[i]));
+            const ff t = two_prod(h, L.v[i].hi);
+            L.x[i] = ff_add_f2(L.x[i], t.hi, __fadd_rn(t.lo, __fmaf_rn(h, L.v[i].lo, dxc[i])));
             L.v[i] = ff_add_f(L.v[i], du[i]);
         }
         if (x1n) {
             L.x[1] = *x1n;
             L.x[2] = *thn;
         }
-        L.lam = ff_add_f(L.lam, h);
+        return after_step(L, I, R, ff_add_f(L.lam, h));
+    }
+
+    // Geodesic::Update after the integrator (Geodesic.cpp:66-87): the new affine
+    // parameter, the step count, terminations, diagnostics.
+    static __device__ __forceinline__ bool after_step(Lane& L, const ImageConst& I, const RunConst& R, ff lam) {
+        L.lam = lam;
         ++L.steps;
         L.term = terms(L, I, R);
         diags(L, I, R, false);

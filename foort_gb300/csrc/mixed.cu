@@ -62,6 +62,8 @@ void fill_mixed_constants(int metric_id, ImageConst& ic, const RunConst& rc) {
     // right-hand side is always taken in FP64
     if (metric_id == kMankoNovikov) r_fp64 = std::max(r_fp64, mn_fp64_radius(ic.m, kMnMaxFp32Exponent));
     mx.r_fp64 = r_fp64 > 0.0 ? static_cast<float>(coord(r_fp64)) : 0.f;
+    // FP64-analytic: every step in FP64 (x1 < +inf holds for every finite position)
+    if (rc.precision == FOORT_PREC_FP64_ANALYTIC) mx.r_fp64 = HUGE_VALF;
     const double rh = ic.m.rh;
     ff_split(coord(rh * (1 + ic.h_eps)), mx.hthr[0], mx.hthr[1]);
     ff_split(ic.h_eps > 0 ? coord(ic.h_eps) : (rlog ? -HUGE_VAL : 0.0), mx.hthr0[0], mx.hthr0[1]);

@@ -54,13 +54,20 @@ extern "C" {
 /* Arithmetic of the integration kernel */
 #define FOORT_PREC_FP64 0  /* every operation in FP64, finite-difference Christoffels   */
 #define FOORT_PREC_MIXED 1 /* FP32 bulk with compensated state, FP64 where needed       */
+/* Every step in FP64 with the analytic derivatives of the mixed kernel (its step_fp64):
+ * the all-FP64 reference of the mixed kernel's own formulation, against which its
+ * rounding error is measured. The reference's finite differences (FOORT_PREC_FP64,
+ * Metric.cpp:14-55, h = 1e-7) lose digits where the metric is nearly constant: at
+ * r ~ 100 a central difference of g_tt ~ -1 + 2/r keeps ~6 of its 16 digits. Engine
+ * extension; no counterpart in the reference. */
+#define FOORT_PREC_FP64_ANALYTIC 2
 
 /* Options of the mixed-precision kernel (engine extension). By default its decisions
  * (terminations, equator crossings, closest radius) are taken by float-float
  * comparisons of its compensated (48-bit) state, which agree with FP64 comparisons
  * except within 2^-48 (relative) of a threshold. */
 #define FOORT_MIXED_FP64_DECISIONS 0x1u    /* take them in FP64 on the exact double value  */
-#define FOORT_MIXED_FP64_NEAR_HORIZON 0x2u /* FP64 right-hand side near the horizon       */
+#define FOORT_MIXED_FP64_NEAR_HORIZON 0x2u /* whole steps in FP64 inside r_+ + margin       */
 
 /* TermBitflag, Terminations.h:29-33 */
 #define FOORT_TERM_BOUNDARY_SPHERE 0x1u
@@ -142,7 +149,7 @@ typedef struct foort_run_desc {
     uint64_t geopos_output_steps;
 
     double mixed_fp64_margin;        /* with FOORT_MIXED_FP64_NEAR_HORIZON: lanes with
-                                        r < r_+ + margin evaluate the RHS in FP64       */
+                                        r < r_+ + margin take the whole step in FP64    */
 
     uint32_t n_images;               /* >= 1                                          */
     uint32_t reserved1;
@@ -183,6 +190,8 @@ typedef struct foort_stats {
     uint32_t n_blocks;
     uint32_t block_size;
     uint32_t lanes_per_geodesic; /* 1, or 2 where two lanes integrated each geodesic   */
+    uint32_t refill_steps;   /* the launch's regrouping cadence (foort_launch_shape)   */
+    uint32_t poll_steps;     /* its steps between budget / cancel polls               */
 } foort_stats;
 
 typedef struct foort_ctx foort_ctx;
@@ -268,7 +277,9 @@ int foort_gpu_set_budget(foort_ctx* ctx, uint64_t max_total_steps);
  * kernel every few hundred steps). Safe to call from another host thread. */
 int foort_gpu_cancel(foort_ctx* ctx);
 
-/* Launch shape override (0 = autotuned default). */
+/* Launch shape override: CTA size (a multiple of 32, at most 128) and a cap on resident
+ * CTAs per SM; 0 leaves each to the autotuner's cached shape for the launch, or to the
+ * built-in rule (128 threads, as many CTAs as fit) where the cache has none. */
 int foort_gpu_set_launch(foort_ctx* ctx, uint32_t block_size, uint32_t blocks_per_sm);
 
 /* Lanes per geodesic in mixed precision with RK4 and the Kerr or flat metric: 0 chooses
@@ -278,6 +289,57 @@ int foort_gpu_set_launch(foort_ctx* ctx, uint32_t block_size, uint32_t blocks_pe
  * are the same either way. No counterpart in the reference (one OpenMP thread per
  * geodesic, Main.cpp:327-414). */
 int foort_gpu_set_lanes(foort_ctx* ctx, uint32_t lanes_per_geodesic);
+
+/* ---- launch shapes and the autotuner --------------------------------------------------
+ * A launch shape is the CTA size, a cap on resident CTAs per SM, the lanes per geodesic,
+ * the regrouping cadence -- how many steps a warp integrates before it refills lanes whose
+ * geodesics ended -- and how many steps pass between polls of the step budget and the
+ * cancel flag. Results do not depend on the shape: every geodesic goes through the same
+ * arithmetic wherever it runs. Only the time does, and the autotuner measures it.
+ * Engine extension: the reference's round loop is an OpenMP for with the static schedule
+ * (Main.cpp:348). */
+typedef struct foort_launch_shape {
+    uint32_t block_size;    /* threads per CTA: 32, 64, 96 or 128                      */
+    uint32_t blocks_per_sm; /* cap on resident CTAs per SM (0 = as many as fit)        */
+    uint32_t lanes;         /* lanes per geodesic: 1, or 2 where the kernel has two    */
+    uint32_t refill_steps;  /* >= 1: steps a warp runs between refills of idle lanes   */
+    uint32_t poll_steps;    /* >= 1: steps between budget / cancel polls               */
+    uint32_t reserved;
+    double ms;              /* the search's measured time for this shape (0: none)     */
+} foort_launch_shape;
+
+/* Autotune the launch of n pixels held in DEVICE memory: time candidate shapes with CUDA
+ * events on `cuda_stream` (lanes x CTA size, then the regrouping cadence and the poll
+ * interval around the best), on all n pixels or, for launches of more than
+ * FOORT_TUNE_SAMPLE_LANES_X times the resident lanes, on a prefix of that many. The
+ * fastest goes into the launch-shape cache under this context's key for n (see
+ * foort_tune_key) and into *best (may be NULL). The call ends with a launch of all n
+ * pixels in the best shape, so d_out holds their results as after
+ * foort_gpu_integrate_async. Synchronous. */
+#define FOORT_TUNE_SAMPLE_LANES_X 4u
+int foort_gpu_autotune(foort_ctx* ctx, const foort_pixel* d_px, uint64_t n, foort_result* d_out,
+                       void* cuda_stream, foort_launch_shape* best);
+
+/* on = 1: a launch whose key has no cache entry first runs the search (that launch waits
+ * for its stream and takes several times longer); on = 0 (default): launches use the
+ * cached shape where there is one and the built-in rule elsewhere. */
+int foort_gpu_set_autotune(foort_ctx* ctx, int32_t on);
+
+/* The shape a launch of n pixels would use now (cache, overrides, built-in rule). */
+int foort_gpu_launch_shape(foort_ctx* ctx, uint64_t n, foort_launch_shape* shape);
+
+/* The launch-shape cache: one table per process, shared by every context. A key names
+ * the GPU's SM count, the kernel variant (metric, integrator, precision, log-r, FP64
+ * decisions, strong-field FP64 region) and the size bucket floor(log2 n) of the launch.
+ * save / load write and read one text line per entry (load adds to the table). */
+uint32_t foort_tune_bucket(uint64_t n);
+int foort_tune_key(const foort_run_desc* desc, int32_t num_sms, uint64_t n, char* buf, uint64_t cap);
+int foort_tune_put(const char* key, const foort_launch_shape* shape);
+int foort_tune_get(const char* key, foort_launch_shape* shape); /* FOORT_E_BADARG: no entry */
+uint64_t foort_tune_count(void);
+void foort_tune_clear(void);
+int foort_tune_save(const char* path);
+int foort_tune_load(const char* path);
 
 int foort_gpu_get_stats(const foort_ctx* ctx, foort_stats* stats);
 

@@ -18,7 +18,9 @@ import numpy as np
 from foort_gb300 import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = "/root/reference/FOORT"
+# The reference's FOORT source directory (its .cpp / .h files and Output/), for the `ref`
+# targets of the Makefile and the fixtures; FOORT_REFERENCE_SRC overrides the default.
+REF_SRC = os.environ.get("FOORT_REFERENCE_SRC", "/root/reference/FOORT")
 
 _LIBS = {}
 
@@ -28,7 +30,7 @@ def build(with_ref=None, quiet=True):
     if with_ref is None:
         with_ref = os.path.isdir(REF_SRC)
     targets = ["all"] + (["ref"] if with_ref else [])
-    out = subprocess.run(["make", "-j8", "-C", HERE] + targets, capture_output=True, text=True)
+    out = subprocess.run(["make", "-j8", "-C", HERE, f"REF={REF_SRC}"] + targets, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout[-3000:] + out.stderr[-3000:])
     return out

@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 from foort_gb300 import abi, workloads  # noqa: E402
 
-OUTDIR = "/root/reference/FOORT/Output"
+OUTDIR = os.path.join(oracle.REF_SRC, "Output")
 
 
 def shipped_dat():

@@ -221,3 +221,50 @@ def test_plugin_derivatives_near_the_horizon(engine_lib, metric, params):
     print(f"metric {metric} {params}: {checked} points, worst relative difference {worst:.2e}")
     assert checked >= 20, checked
     assert worst < 1e-10, worst
+
+
+MN_RADIUS_CHECK = r"""
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include "analytic_metric.cuh"
+using namespace foort;
+// The first radius, scanning inward with r - r_+ shrinking by 0.99 per step, at which an
+// exponent exceeds 8 on a 0.25-degree theta grid; r_+ if none does down to r_+ + 1e-9.
+static double fine_radius(const MetricConst& M) {
+    const double rp = 1.0 + M.q[3];
+    for (double d = 1e4 - rp; d > 1e-9; d *= 0.99)
+        if (!(mn_max_exponent(M, rp + d, 720) <= kMnMaxFp32Exponent)) return rp + d;
+    return rp;
+}
+int main(int argc, char** argv) {
+    for (int i = 1; i + 1 < argc; i += 2) {
+        const double p[6] = {std::atof(argv[i]), std::atof(argv[i + 1]), 0, 0, 0, 0};
+        const MetricConst M = make_metric_const(kMankoNovikov, p);
+        std::printf("%s %s %.17g %.17g %.17g\n", argv[i], argv[i + 1], 1.0 + M.q[3],
+                    mn_fp64_radius(M, kMnMaxFp32Exponent), fine_radius(M));
+    }
+}
+"""
+
+
+def test_manko_novikov_fp64_radius_covers_a_fine_scan(tmp_path):
+    """The mixed kernel takes Manko-Novikov steps in FP64 inside the radius where one of
+    the metric's exponents exceeds 8 (mn_fp64_radius: 1-degree theta grid, r - r_+
+    shrinking by 0.8 per step, then bisection and a 10 % margin). A coarse scan could
+    step over a narrow band where an exponent peaks; the radius must still enclose the
+    first such radius that a 0.25-degree grid with 1 % radial steps finds."""
+    src = tmp_path / "mn_radius.cpp"
+    src.write_text(MN_RADIUS_CHECK)
+    exe = tmp_path / "mn_radius"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "foort_gb300", "csrc"),
+                    "-o", str(exe), str(src)], check=True)
+    rng = np.random.default_rng(5)
+    sets = [(0.94, 13.0), (0.9, 5.0), (0.7, 1.0), (0.5, -3.0), (0.99, 20.0), (0.2, 0.5)]
+    sets += [(float(rng.uniform(0.05, 0.99)), float(rng.uniform(-20.0, 20.0))) for _ in range(10)]
+    args = [f"{v:.17g}" for s in sets for v in s]
+    out = subprocess.run([str(exe)] + args, check=True, capture_output=True, text=True).stdout
+    for line in out.strip().splitlines():
+        a, a3, rp, coarse, fine = line.split()
+        print(f"a={a} alpha3={a3}: r_+ {float(rp):.6f}, FP64 radius {float(coarse):.6f}, fine scan {float(fine):.6f}")
+        assert float(coarse) >= float(fine), line
