@@ -23,7 +23,8 @@ mixed kernel's derivatives) on all pixels; per-pixel condition numbers from two 
 launches; error reports of mixed and plain FP64 against the oracle (foort_gb300.accuracy).
 N > 1 (torchrun): every rank integrates its own copy of the workload (weak scaling,
 no collective on the data path); times are the max over ranks. The FP64 and CPU legs
-run at N = 1 only.
+run at N = 1 only. --shard: one run split over the ranks instead, each round gathered
+before the mesh picks the next (strong scaling).
 --impl reference: the reference's algorithm on the host cores (the oracle's
 restatement built with the reference's -Ofast flags; the reference itself only builds
 where its sources are), on a bounded seeded sample of the pixels the reference's own
@@ -147,32 +148,6 @@ def kind_of(wl):
     return m, i
 
 
-def run_meshes(eng_mod, e, wl, integrate, on_round=None):
-    """One FOORT run (Main.cpp:313-419) of every image of the workload, the images'
-    meshes advancing in lockstep so that each round is one launch over all images.
-    integrate(px) -> results; on_round(px, res) is called after each round."""
-    meshes = [eng_mod.Mesh.from_spec(spec, wl.desc.diag_flags, wl.desc.value_diag) for spec in wl.mesh]
-    n_rounds = 0
-    while True:
-        live = [(i, m) for i, m in enumerate(meshes) if not m.finished()]
-        if not live:
-            break
-        parts = [m.pixels(image=i) for i, m in live]
-        px = np.concatenate(parts)
-        res = integrate(px)
-        k = 0
-        for (i, m), p in zip(live, parts):
-            m.set_results(res[k:k + len(p)])
-            m.end_round()
-            k += len(p)
-        if on_round:
-            on_round(px, res)
-        n_rounds += 1
-    for m in meshes:
-        m.close()
-    return n_rounds
-
-
 def adaptive_rounds(eng_mod, wl, results_out=None):
     """The pixel list of every round of the workload (one run with the engine)."""
     px_rounds = []
@@ -181,7 +156,7 @@ def adaptive_rounds(eng_mod, wl, results_out=None):
             px_rounds.append(px.copy())
             if results_out is not None:
                 results_out.append(res.copy())
-        run_meshes(eng_mod, e, wl, e.integrate, keep)
+        eng_mod.run_rounds(wl.mesh, wl.desc, e.integrate, keep)
     return px_rounds
 
 
@@ -275,6 +250,57 @@ def run_reference(args, rank):
     return 0
 
 
+def run_sharded(args, rank, world, local):
+    """--shard: ONE run of the workload split over the ranks (strong scaling). Every rank
+    holds the same mesh; each round, each rank integrates its contiguous slice through the
+    C ABI from host memory and the slices are gathered before the mesh ends the round
+    (foort_gb300.multirank.sharded_run). value = the run's geodesics / the slowest rank's
+    time per run."""
+    import torch
+    import foort_gb300
+    from foort_gb300 import abi, multirank
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    wl = workload(args.workload, abi.PREC_MIXED, args.iteration_pixels)
+    with foort_gb300.Engine(wl.desc) as e:
+        def one_run():
+            n = [0, 0]
+
+            def count(px, res):
+                n[0] += len(px)
+                n[1] += 1
+            multirank.sharded_run(wl.mesh, wl.desc, e.integrate, rank, world, dist, on_round=count)
+            return n
+        for _ in range(args.warmup):
+            n_geod, n_rounds = one_run()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            one_run()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t = multirank.max_over_ranks((time.perf_counter() - t0) / args.steps, dist, device="cuda")
+    value = n_geod / t
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "mixed-f32", "data": "synthetic", "mode": "sharded",
+            "config": dict(config_block(wl, args, rounds=n_rounds, geod=n_geod), parallelism=f"shard{world}"),
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": n_geod * abi.PIXEL_DTYPE.itemsize,
+                    "d2h_bytes_per_step": n_geod * abi.RESULT_DTYPE.itemsize},
+            "gpu_launches": args.steps * n_rounds}), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_profile_case(args):
     """One warm-up and one measured launch per precision on a seeded sample of the grid."""
     import foort_gb300
@@ -361,6 +387,9 @@ def main():
     ap.add_argument("--iteration-pixels", type=int, default=None)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison leg")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--shard", action="store_true",
+                    help="one run split over the ranks, gathered each round (strong scaling) instead of one "
+                         "independent run per rank")
     ap.add_argument("--no-tune", action="store_true",
                     help="use the built-in launch rule instead of autotuning each round in the first warm-up step")
     ap.add_argument("--cpu-seconds", type=float, default=None,
@@ -378,6 +407,8 @@ def main():
         return run_reference(args, rank)
     if args.profile:
         return run_profile_case(args)
+    if args.shard:
+        return run_sharded(args, rank, world, local)
 
     import torch
     import foort_gb300
@@ -489,7 +520,7 @@ def main():
             state["r"] += 1
             return ov
 
-        run_meshes(foort_gb300, e, wl, integrate)
+        foort_gb300.run_rounds(wl.mesh, wl.desc, integrate)
 
     with foort_gb300.Engine(wl.desc) as e:
         e.set_lanes(args.lanes)

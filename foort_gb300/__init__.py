@@ -463,6 +463,35 @@ def config_mesh(cfg):
     return m
 
 
+def run_rounds(mesh_specs, desc, integrate, on_round=None):
+    """One FOORT run (the round loop of Main.cpp:313-419) over one mesh per image, the
+    images' meshes advancing in lockstep so that each round is one integrate() call over
+    the pixels of every unfinished image. mesh_specs: Mesh.from_spec specs; integrate(px)
+    -> results; on_round(px, res) after each round. Returns the number of rounds."""
+    meshes = [Mesh.from_spec(spec, desc.diag_flags, desc.value_diag) for spec in mesh_specs]
+    n_rounds = 0
+    try:
+        while True:
+            live = [(i, m) for i, m in enumerate(meshes) if not m.finished()]
+            if not live:
+                break
+            parts = [m.pixels(image=i) for i, m in live]
+            px = np.concatenate(parts)
+            res = integrate(px)
+            k = 0
+            for (i, m), p in zip(live, parts):
+                m.set_results(res[k:k + len(p)])
+                m.end_round()
+                k += len(p)
+            if on_round:
+                on_round(px, res)
+            n_rounds += 1
+    finally:
+        for m in meshes:
+            m.close()
+    return n_rounds
+
+
 def run_config(path, precision=abi.PREC_MIXED, output_dir=None):
     """A whole FOORT run from a .cfg file: the configured metric, diagnostics,
     terminations, view screen, mesh, integrator and output files (Main.cpp:161-424), on

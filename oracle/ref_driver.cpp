@@ -22,6 +22,7 @@
 #include "ViewScreen.h"
 
 #include "../include/foort_gpu.h"
+#include "ref_driver.h"
 
 #include <omp.h>
 
@@ -192,31 +193,20 @@ int ref_integrate(const foort_run_desc* d, const foort_pixel* px, uint64_t n, fo
     return FOORT_OK;
 }
 
-// Mesh description for ref_run / ref_mesh_trace.
-typedef struct ref_mesh_spec {
-    int32_t kind;  // 0 SimpleSquareMesh, 1 SquareSubdivisionMeshV2
-    int32_t max_subdivide;
-    uint64_t total_pixels;
-    uint64_t max_pixels;
-    uint64_t initial_pixels;
-    uint64_t iteration_pixels;
-    int32_t initial_sub_to_final;
-    int32_t reserved;
-} ref_mesh_spec;
-
 static std::unique_ptr<Mesh> make_mesh(const ref_mesh_spec* ms, DiagBitflag vd) {
     if (ms->kind == 0) return std::unique_ptr<Mesh>(new SimpleSquareMesh(ms->total_pixels, vd));
     return std::unique_ptr<Mesh>(new SquareSubdivisionMeshV2(ms->max_pixels, ms->initial_pixels, ms->max_subdivide,
                                                              ms->iteration_pixels, ms->initial_sub_to_final != 0, vd));
 }
 
+}  // extern "C"
+
 // A full run of image 0 as Main.cpp:313-427 does it, writing the reference's .dat files
-// through GeodesicOutputHandler. Returns the number of geodesics and the wall time.
-int ref_run(const foort_run_desc* d, const ref_mesh_spec* ms, const char* prefix, const char* timestamp,
-            const char* ext, uint64_t to_cache, uint64_t per_file, int32_t first_line, int nthreads,
-            uint64_t* n_geod, uint32_t* n_rounds, double* seconds) {
+// through GeodesicOutputHandler; each round's geodesics are integrated by `body`.
+int ref_run_rounds(const foort_run_desc* d, const ref_mesh_spec* ms, const char* prefix, const char* timestamp,
+                   const char* ext, uint64_t to_cache, uint64_t per_file, int32_t first_line, const RefRoundBody& body,
+                   uint64_t* n_geod, uint32_t* n_rounds, double* seconds) {
     if (!d || !ms || !d->images) return FOORT_E_BADARG;
-    if (nthreads <= 0) nthreads = omp_get_max_threads();
     const foort_image_desc& I = d->images[0];
     std::unique_ptr<Metric> M = make_metric(d, I.metric_params);
     std::unique_ptr<Source> S(new NoSource(M.get()));
@@ -234,14 +224,33 @@ int ref_run(const foort_run_desc* d, const ref_mesh_spec* ms, const char* prefix
     uint64_t total = 0;
     uint32_t rounds = 0;
     while (!view->IsFinished()) {
-        long long N = static_cast<long long>(view->getCurNrGeodesics());
-        total += static_cast<uint64_t>(N);
+        total += static_cast<uint64_t>(view->getCurNrGeodesics());
         ++rounds;
+        const int rc = body(view.get(), &outh, RefRunObjects{M.get(), S.get(), diags, vd, terms, integ});
+        if (rc != FOORT_OK) return rc;
+        view->EndCurrentLoop();
+    }
+    outh.OutputFinished();
+    if (n_geod) *n_geod = total;
+    if (n_rounds) *n_rounds = rounds;
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return FOORT_OK;
+}
+
+extern "C" {
+
+// ref_run_rounds with the reference's own round body: the OpenMP loop of Main.cpp:327-402.
+int ref_run(const foort_run_desc* d, const ref_mesh_spec* ms, const char* prefix, const char* timestamp,
+            const char* ext, uint64_t to_cache, uint64_t per_file, int32_t first_line, int nthreads,
+            uint64_t* n_geod, uint32_t* n_rounds, double* seconds) {
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+    auto body = [nthreads](ViewScreen* view, GeodesicOutputHandler* outh, const RefRunObjects& o) {
+        long long N = static_cast<long long>(view->getCurNrGeodesics());
 #pragma omp parallel num_threads(nthreads)
         {
 #pragma omp single
-            outh.PrepareForOutput(static_cast<largecounter>(N));
-            Geodesic g(M.get(), S.get(), diags, vd, terms, integ);
+            outh->PrepareForOutput(static_cast<largecounter>(N));
+            Geodesic g(o.metric, o.source, o.diags, o.valdiag, o.terms, o.integrator);
 #pragma omp for schedule(dynamic, 4)
             for (long long k = 0; k < N; ++k) {
                 Point p;
@@ -251,16 +260,13 @@ int ref_run(const foort_run_desc* d, const ref_mesh_spec* ms, const char* prefix
                 g.Reset(si, p, v);
                 while (g.getTermCondition() == Term::Continue) g.Update();
                 view->GeodesicFinished(static_cast<largecounter>(k), g.getDiagnosticFinalValue());
-                outh.NewGeodesicOutput(static_cast<largecounter>(k), g.getAllOutputStr());
+                outh->NewGeodesicOutput(static_cast<largecounter>(k), g.getAllOutputStr());
             }
         }
-        view->EndCurrentLoop();
-    }
-    outh.OutputFinished();
-    if (n_geod) *n_geod = total;
-    if (n_rounds) *n_rounds = rounds;
-    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    return FOORT_OK;
+        return static_cast<int>(FOORT_OK);
+    };
+    return ref_run_rounds(d, ms, prefix, timestamp, ext, to_cache, per_file, first_line, body, n_geod, n_rounds,
+                          seconds);
 }
 
 // The run-description line the reference writes first in every output file

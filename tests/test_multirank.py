@@ -61,3 +61,68 @@ def test_sharded_round_over_two_gloo_ranks(oracle_mod, tmp_path):
         for name in abi.RESULT_DTYPE.names:
             np.testing.assert_array_equal(got[name], want[name], err_msg=name)
         assert float((tmp_path / f"rank{r}.txt").read_text()) == 2.0  # max over ranks
+
+
+def _c2_shaped():
+    """C2's shape at a size the oracle runs in seconds: Kerr a = 0.99 at 60 deg with a
+    SquareSubdivisionMeshV2 (9^2 seed, MaxSubdivide 3: grid 33; 24 pixels per refinement
+    round), camera and boundary sphere at r = 60 so that each ray is short."""
+    wl = workloads.c2()
+    d = wl.desc
+    d.boundary_radius = 60.0
+    keep = abi.attach_images(d, [abi.make_image((0.99,), r=60.0, theta=60 * workloads.DEG, half_width=12.0)])
+    mesh = [("v2", dict(max_pixels=0, initial_pixels=81, max_subdivide=3, iteration_pixels=24,
+                        initial_sub_to_final=0))]
+    return d, mesh, keep
+
+
+def _run_main(rank, world, port, outdir):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        import oracle
+        d, mesh, keep = _c2_shaped()
+        seen, mine = [], []
+
+        def integrate(p):
+            mine.append(len(p))
+            return oracle.integrate(d, p, fast=False, nthreads=1)
+
+        rounds = multirank.sharded_run(mesh, d, integrate, rank, world, dist,
+                                       on_round=lambda px, res: seen.append((px.copy(), res.copy())))
+        np.savez(os.path.join(outdir, f"run{rank}.npz"), px=np.concatenate([p for p, _ in seen]),
+                 res=np.concatenate([r for _, r in seen]), sizes=np.array([len(p) for p, _ in seen]),
+                 mine=np.array(mine), rounds=rounds)
+        del keep
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_c2_shaped_run_hands_out_the_single_rank_pixels(oracle_mod, tmp_path):
+    """A whole adaptive run (Main.cpp:313-419) over two gloo ranks, each integrating its
+    contiguous half of every round with the oracle and gathering before the mesh ends the
+    round (Mesh.cpp:1092-1186), must hand out the same pixels in the same order, with the
+    same results, as the run on one rank; each rank integrated only its half."""
+    import foort_gb300
+    import torch.multiprocessing as mp
+    world = 2
+    mp.start_processes(_run_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    d, mesh, keep = _c2_shaped()
+    seen = []
+    rounds = foort_gb300.run_rounds(mesh, d, lambda p: oracle_mod.integrate(d, p, fast=False),
+                                    on_round=lambda px, res: seen.append((px.copy(), res.copy())))
+    want_px = np.concatenate([p for p, _ in seen])
+    want_res = np.concatenate([r for _, r in seen])
+    sizes = [len(p) for p, _ in seen]
+    assert rounds >= 3 and sizes[0] == 81, sizes
+    for r in range(world):
+        f = np.load(tmp_path / f"run{r}.npz")
+        assert int(f["rounds"]) == rounds and list(f["sizes"]) == sizes
+        for name in abi.PIXEL_DTYPE.names:
+            np.testing.assert_array_equal(f["px"][name], want_px[name], err_msg=name)
+        for name in abi.RESULT_DTYPE.names:
+            np.testing.assert_array_equal(f["res"][name], want_res[name], err_msg=name)
+        halves = [multirank.shard_range(n, r, world) for n in sizes]
+        assert list(f["mine"]) == [hi - lo for lo, hi in halves]
+    del keep
