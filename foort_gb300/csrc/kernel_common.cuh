@@ -125,16 +125,6 @@ __device__ __forceinline__ void geopos_sample(GeoposRec& g, const RunConst& R, c
     d[3] = x[3];
 }
 
-// The GeodesicPosition record of the calling lane. It lives in shared memory, one per
-// thread of a CTA of at most 128 (every launch path caps the CTA there), because only the
-// second pass writes it: kept in the lane state, its ten words cost the first pass's
-// step loop registers on every step (the C4 kernel spilled them). A lane flag says
-// whether the record is live.
-__device__ __forceinline__ GeoposRec& lane_geopos() {
-    __shared__ GeoposRec rec[128];
-    return rec[threadIdx.x];
-}
-
 // FourColorScreenDiagnostic::UpdateData, Diagnostics.cpp:159-200 (only on BoundarySphere)
 static __device__ __noinline__ int32_t four_color_quadrant(double th, double ph) {
     if (fabs(ph) < 2 * kRefPi * 1e5) {
@@ -258,8 +248,6 @@ __device__ __forceinline__ bool finite4(const double a[4]) {
 //   finish(L, R, out)                  write the lane's record
 //   stop(L, R, out, err)               write a partial record (budget / cancel)
 //   counters: L.rhs, L.fp64            accumulated per lane, flushed at each poll
-//   L.gp_on                            set by the loop before init: record GeodesicPosition
-//                                      samples in lane_geopos()
 //
 // Every warp takes pixels from one global counter (one atomic per warp, shared by the
 // lanes that need work) and keeps integrating until the queue is empty. Lanes whose
@@ -316,9 +304,9 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                             idx = my;
                             // i and cnt start at 0 as literals: copying them from the record
                             // made the C4 kernel 3 % slower on GB300
-                            L.gp_on = A.gp_plan && !odd && A.gp_plan[my].M > 0 && A.gp_plan[my].j > 0;
-                            if (L.gp_on)
-                                lane_geopos() = GeoposRec{A.gp_plan[my].dst, A.gp_plan[my].j, A.gp_plan[my].M, 0, 0};
+                            L.gp = (A.gp_plan && !odd && A.gp_plan[my].M > 0 && A.gp_plan[my].j > 0)
+                                       ? GeoposRec{A.gp_plan[my].dst, A.gp_plan[my].j, A.gp_plan[my].M, 0, 0}
+                                       : GeoposRec{nullptr, 1, 0, 0, 0};
                             E::init(L, A.images[p.image], R, p);
                             active = true;
                         }

@@ -80,7 +80,7 @@ struct Fp64Engine {
         uint32_t rhs = 0;
         uint32_t fp64 = 0;
         int32_t term = 0;
-        bool gp_on;  // set by the loop before init: GeodesicPosition is recorded
+        GeoposRec gp;  // set by the loop before init (dst null: not recording)
         FdParts P;     // Verlet: the parts at x (computed at the previous step's new position)
     };
 
@@ -93,7 +93,7 @@ struct Fp64Engine {
         L.term = FOORT_TERMCODE_CONTINUE;
         L.img = p.image;
         reset_lane_state(R, L.x, L.D, L.T);
-        if (L.gp_on) geopos_sample(lane_geopos(), R, L.x, 0.0, FOORT_TERMCODE_CONTINUE);  // Geodesic::Reset's sample
+        if (L.gp.dst) geopos_sample(L.gp, R, L.x, 0.0, FOORT_TERMCODE_CONTINUE);  // Geodesic::Reset's sample
     }
 
     // One Geodesic::Update (Geodesic.cpp:61-88). Returns false once the geodesic ends.
@@ -173,7 +173,7 @@ struct Fp64Engine {
         const double r = radius_of(R, L.x[1]);
         L.term = check_terms(R, M.rh, I.h_eps, r, L.x[2], L.T);
         update_diags(R, r, L.x[2], L.x[3], L.lam, L.term, L.D);
-        if (L.gp_on) geopos_sample(lane_geopos(), R, L.x, L.lam, L.term);
+        if (L.gp.dst) geopos_sample(L.gp, R, L.x, L.lam, L.term);
         if (!(finite4(L.x) && finite4(L.v))) {
             // The reference keeps integrating a non-finite state until TimeOut fires;
             // without TimeOut it would never stop, so the lane stops here.

@@ -327,7 +327,7 @@ struct MixedEngine {
     struct Lane {
         ff x[4], v[4];
         ff lam;
-        uint32_t steps;  // a geodesic's steps (TimeOut limits of 2^32 or more are out of range)
+        uint64_t steps;
         TermState T;
         // diagnostics on the compensated state
         int32_t quad, passes;
@@ -340,7 +340,7 @@ struct MixedEngine {
         uint32_t rhs = 0;
         uint32_t fp64 = 0;
         int32_t term = 0;
-        bool gp_on;  // set by the loop before init: GeodesicPosition is recorded
+        GeoposRec gp;  // set by the loop before init (dst null: not recording)
         MetricAt<float> mc;  // Verlet: the metric part at the current (x1, theta)
     };
 
@@ -364,7 +364,7 @@ struct MixedEngine {
         double x[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) x[i] = ff_d(L.x[i]);
-        geopos_sample(lane_geopos(), R, x, lam, L.term);
+        geopos_sample(L.gp, R, x, lam, L.term);
     }
 
     static __device__ __forceinline__ void load_double(const Lane& L, double x[4], double v[4]) {
@@ -397,7 +397,7 @@ struct MixedEngine {
         L.T.tcur = 0;
         if (verlet_cached(I)) L.mc = metric(I, R.rlog != 0, L.x[1], L.x[2]);
         diags(L, I, R, true);  // Geodesic::Reset's start sample at lambda = 0
-        if (L.gp_on) geopos(L, R, 0.0);
+        if (L.gp.dst) geopos(L, R, 0.0);
     }
 
     // EquatorialPasses and ClosestRadius updates (Diagnostics.cpp:351-380, :427-446) on
@@ -809,7 +809,7 @@ struct MixedEngine {
         ++L.steps;
         L.term = terms(L, I, R);
         diags(L, I, R, false);
-        if (L.gp_on) geopos(L, R, 1.0);  // lambda > 0 after a step; only compared with 0
+        if (L.gp.dst) geopos(L, R, 1.0);  // lambda > 0 after a step; only compared with 0
         // A NaN or Inf anywhere in the state reaches r or u^r within one step through the
         // right-hand side, so those two words stand for the whole state here; the full
         // state is checked again when the geodesic's record is written.

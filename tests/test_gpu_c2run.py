@@ -13,7 +13,11 @@ hand out the same pixels exactly as long as every quadrant agreed. The test asse
   quadrant that disagrees comes before that point (a sequence that changes without
   one is a mesh error);
 * the quadrants of the common part agree on >= 99.9 % of pixels, and every
-  disagreement lies on a decision boundary (accuracy.explain_mismatches);
+  disagreement lies on a decision boundary (parity.explain_mismatches) or on a ray
+  whose end point the FP64 algorithm itself does not determine: the reference's
+  finite-difference FP64 kernel and the all-FP64 analytic kernel disagree on it by more
+  than 1e-4 (parity.fp64_ill_posed; the screen row through the rotation axis), at most
+  one such pixel per 10,000;
 * the closest radii agree with the reference's "%f" text (6 decimals: 3e-8 relative
   at the median radius): FP64 kernel median < 1e-7 and p99 < 1e-6 relative, the level
   at which the reference's own -Ofast and strict builds differ on strongly lensed rays;
@@ -72,8 +76,11 @@ def test_c2_run_matches_the_reference_run(engine_lib, oracle_mod, precision):
     assert 1.0 - quad_mism.mean() >= parity.MIN_DISCRETE_AGREEMENT
     if quad_mism.any():
         wl.desc.precision = abi.PREC_FP64
-        unexplained = parity.explain_mismatches(oracle_mod, wl.desc, px[:split], res[:split], quad_mism)
+        unexplained, ill = parity.explain_or_ill_posed(oracle_mod, wl.desc, px[:split], res[:split], quad_mism)
+        print(f"{len(ill)} disagreement(s) where the two FP64 kernels disagree by more than "
+              f"{parity.FP64_ILL_POSED:g}: {px[:split][ill]}")
         assert len(unexplained) == 0, px[:split][unexplained]
+        assert len(ill) <= max(1, split // 10000)
 
     # closest radius, on the common part where the quadrants agree
     keep = ~quad_mism

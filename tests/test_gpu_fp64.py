@@ -4,6 +4,7 @@ Every call goes through the C ABI (libfoort_gpu.so). The rules are in tests/pari
 >= 99.9 % discrete agreement with every disagreement on a decision boundary, and the
 endpoint error stated per case.
 """
+import ctypes as C
 import os
 
 import numpy as np
@@ -155,7 +156,8 @@ def test_cancel_from_host(eng):
         t.join()
         st = e.stats()
     print(f"cancelled after {dt:.2f} s: {st['geodesics']} of {len(px)} geodesics finished")
-    assert st["status"] == abi.FOORT_E_CANCELLED, f"the launch ended ({dt:.2f} s) without seeing the cancel flag"
+    status = C.c_int32(st["status"]).value  # foort_stats.status holds the FOORT_E_* code in a uint32
+    assert status == abi.FOORT_E_CANCELLED, f"the launch ended ({dt:.2f} s) without seeing the cancel flag"
     assert dt < 3.0
     assert np.any(res["err"] & abi.ERR_CANCELLED)
     stopped = (res["err"] & (abi.ERR_CANCELLED | abi.ERR_UNFINISHED)) != 0
