@@ -33,6 +33,7 @@ PREC_FP64_ANALYTIC = 2  # every step in FP64 with the mixed kernel's analytic de
 
 MIXED_FP64_DECISIONS = 0x1
 MIXED_FP64_NEAR_HORIZON = 0x2
+MIXED_FP64_TURNING_POINTS = 0x4
 
 # foort_gpu_integrate_noalloc: images its static device array has room for
 NOALLOC_MAX_IMAGES = 256

@@ -212,7 +212,9 @@ const void* select_kernel(const RunConst& R) {
 // The two-lanes-per-geodesic kernel for these options, or nullptr (FP64, FP64-analytic,
 // Verlet, the called plugins, the strong-field FP64 steps).
 const void* select_pair_kernel(const RunConst& R) {
-    if (R.precision != FOORT_PREC_MIXED || R.mixed_fp64_margin > 0.0) return nullptr;
+    if (R.precision != FOORT_PREC_MIXED || R.mixed_fp64_margin > 0.0 ||
+        (R.mixed_options & FOORT_MIXED_FP64_TURNING_POINTS))
+        return nullptr;
     return mixed_pair_kernel_variant(R.metric_id, R.integrator, (R.mixed_options & FOORT_MIXED_FP64_DECISIONS) != 0);
 }
 

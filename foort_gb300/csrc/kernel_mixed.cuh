@@ -300,11 +300,12 @@ __device__ __noinline__ StepD step_fp64(const ImageConst& I, const RunConst& R, 
 // below 1, where floats are twice as dense as just above 1, so every other 1/s falls just
 // past a rounding midpoint and rounds up, making h about 3e-8 too large on average; over
 // 10^5 steps that moved C2's end points by 1e-6 on a tenth of its rays. pi - theta is
-// formed in float-float: near the pole both round to the same float, and a zero m would
-// collapse the step to the smallest step size.
+// formed from theta's float-float parts: near the pole both round to the same float, and a
+// zero m would collapse the step to the smallest step size.
 __device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const MixedConst& mc, ff th, const float v[4]) {
-    const ff dpi = ff_add(ff_of(mc.pi), ff_neg(th));
-    const float t = ff_f(th), pt = ff_f(dpi);
+    // pi - theta to float accuracy: near theta = pi the high parts' difference is exact
+    // (Sterbenz) and the low parts carry the rest
+    const float t = ff_f(th), pt = __fadd_rn(__fsub_rn(mc.pi[0], th.hi), __fsub_rn(mc.pi[1], th.lo));
     const float m = (pt < t) ? pt : t;
     const float s1 = __fadd_rn(fabsf(v[1]), 1e-20f);
     const float s2 = __fmul_rn(__fadd_rn(fabsf(v[2]), 1e-20f), rcp(fabsf(m)));
@@ -317,6 +318,10 @@ __device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const Mixe
     const float hmin = mc.hmin;
     return (h < hmin) ? hmin : h;
 }
+
+// FOORT_MIXED_FP64_TURNING_POINTS: FP64 steps where the radial or the polar speed is
+// below this fraction of the ray's angular motion.
+constexpr float kTurningFraction = 0.05f;
 
 template <int MID, int INTEG, bool DECIDE64>
 struct MixedEngine {
@@ -344,10 +349,11 @@ struct MixedEngine {
         MetricAt<float> mc;  // Verlet: the metric part at the current (x1, theta)
     };
 
-    // Verlet keeps the metric part from step to step unless lanes may switch to the FP64
-    // right-hand side near the horizon.
-    static __device__ __forceinline__ bool verlet_cached(const ImageConst& I) {
-        return INTEG == FOORT_INTEGRATOR_VERLET && !(I.mx.r_fp64 > 0.f);
+    // Verlet keeps the metric part from step to step unless lanes may switch to FP64 steps
+    // (the strong-field radius, turning points).
+    static __device__ __forceinline__ bool verlet_cached(const ImageConst& I, const RunConst& R) {
+        return INTEG == FOORT_INTEGRATOR_VERLET && !(I.mx.r_fp64 > 0.f) &&
+               !(R.mixed_options & FOORT_MIXED_FP64_TURNING_POINTS);
     }
 
     // The FP32 metric part at (x1, theta): inlined for the inlined plugins, called otherwise.
@@ -395,7 +401,7 @@ struct MixedEngine {
         L.has_rmin = false;
         L.T.cH = L.T.cB = L.T.cT = L.T.cTh = 0;
         L.T.tcur = 0;
-        if (verlet_cached(I)) L.mc = metric(I, R.rlog != 0, L.x[1], L.x[2]);
+        if (verlet_cached(I, R)) L.mc = metric(I, R.rlog != 0, L.x[1], L.x[2]);
         diags(L, I, R, true);  // Geodesic::Reset's start sample at lambda = 0
         if (L.gp.dst) geopos(L, R, 0.0);
     }
@@ -491,9 +497,20 @@ struct MixedEngine {
     }
 
     // Whether this step is taken in FP64: lanes inside the strong-field radius r_fp64
-    // (ln r in log-r mode; 0 = never), decided on the step's starting position.
-    static __device__ __forceinline__ bool in_fp64_region(const ImageConst& I, const Lane& L) {
-        return I.mx.r_fp64 > 0.f && L.x[1].hi < I.mx.r_fp64;
+    // (ln r in log-r mode; 0 = never), decided on the step's starting state.
+    // With FOORT_MIXED_FP64_TURNING_POINTS, also near a turning point of r or of theta,
+    // measured against the ray's own angular motion w = (u^theta, sin(theta) u^phi): a
+    // radial turning point where |dr/dlambda| < kTurningFraction r |w|, a polar one where
+    // |u^theta| < kTurningFraction |sin(theta) u^phi|.
+    static __device__ __forceinline__ bool in_fp64_region(const ImageConst& I, const RunConst& R, const Lane& L) {
+        if (I.mx.r_fp64 > 0.f && L.x[1].hi < I.mx.r_fp64) return true;
+        if (R.mixed_options & FOORT_MIXED_FP64_TURNING_POINTS) {
+            const float r = R.rlog ? __expf(L.x[1].hi) : L.x[1].hi;
+            const float vr = R.rlog ? fabsf(L.v[1].hi) * r : fabsf(L.v[1].hi);
+            const float vth = fabsf(L.v[2].hi), vph = fabsf(__sinf(L.x[2].hi) * L.v[3].hi);
+            return vr < kTurningFraction * r * (vth + vph) || vth < kTurningFraction * vph;
+        }
+        return false;
     }
 
     // A step in FP64 (step_fp64) applied to the compensated state. `count`: this lane
@@ -522,12 +539,12 @@ struct MixedEngine {
     // out of line: kept in the kernel, its calls' register needs made the C4 (Johannsen,
     // Verlet) kernel 22 % slower on GB300 although it never ran them.
     static __device__ __forceinline__ bool step(Lane& L, const ImageConst& I, const RunConst& R) {
-        if (in_fp64_region(I, L)) return step_d(L, I, R, true);
+        if (in_fp64_region(I, R, L)) return step_d(L, I, R, true);
         float uf[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) uf[i] = ff_f(L.v[i]);
         const float h = adaptive_step_f32(R, I.mx, L.x[2], uf);
-        if (INTEG == FOORT_INTEGRATOR_VERLET && verlet_cached(I)) return step_verlet_cached(L, I, R, h, uf);
+        if (INTEG == FOORT_INTEGRATOR_VERLET && verlet_cached(I, R)) return step_verlet_cached(L, I, R, h, uf);
         if (INTEG == FOORT_INTEGRATOR_RK4 && MixedMetric<MID>::kInline) return step_rk4_inline(L, I, R, h, uf);
         const Incr d = step_general(I, R, L.x[1], L.x[2], L.v[1], L.v[2], F4{uf[0], uf[1], uf[2], uf[3]}, h);
         L.rhs += d.rhs;
@@ -759,10 +776,10 @@ struct MixedEngine {
         accel_part(m, rlog, us, ka);
 #pragma unroll
         for (int i = 0; i < 4; ++i) k2[i] = __shfl_sync(pmask, ka[i], 1, 2);
-        // stages 3 (even lane) and 4 (odd lane)
-        const ff p3r = ff_add_f(L.x[1], hh * (uf[1] + hh * k1[1])), p3t = ff_add_f(L.x[2], hh * (uf[2] + hh * k1[2]));
-        const ff p4r = ff_add_f(L.x[1], h * (uf[1] + hh * k2[1])), p4t = ff_add_f(L.x[2], h * (uf[2] + hh * k2[2]));
-        m = metric_part<MID, float>(I.mx.q, I.mx, rlog, odd ? p4r : p3r, odd ? p4t : p3t);
+        // stages 3 (even lane) and 4 (odd lane): each lane forms only its own position
+        const float dr = odd ? h * (uf[1] + hh * k2[1]) : hh * (uf[1] + hh * k1[1]);
+        const float dt = odd ? h * (uf[2] + hh * k2[2]) : hh * (uf[2] + hh * k1[2]);
+        m = metric_part<MID, float>(I.mx.q, I.mx, rlog, ff_add_f(L.x[1], dr), ff_add_f(L.x[2], dt));
 #pragma unroll
         for (int i = 0; i < 4; ++i) us[i] = uf[i] + hh * k2[i];
         accel_part(m, rlog, us, ka);

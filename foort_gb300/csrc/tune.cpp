@@ -46,7 +46,8 @@ uint32_t foort_tune_bucket(uint64_t n) {
 
 int foort_tune_key(const foort_run_desc* d, int32_t num_sms, uint64_t n, char* buf, uint64_t cap) {
     if (!d || !buf || cap == 0 || num_sms <= 0) return FOORT_E_BADARG;
-    const int region = (d->mixed_options & FOORT_MIXED_FP64_NEAR_HORIZON) && d->mixed_fp64_margin > 0.0;
+    const int region = ((d->mixed_options & FOORT_MIXED_FP64_NEAR_HORIZON) && d->mixed_fp64_margin > 0.0 ? 1 : 0) |
+                       ((d->mixed_options & FOORT_MIXED_FP64_TURNING_POINTS) ? 2 : 0);
     const int decide64 = (d->mixed_options & FOORT_MIXED_FP64_DECISIONS) != 0;
     const int w = std::snprintf(buf, cap, "sm%d:m%d:i%d:p%d:r%d:d%d:f%d:b%u", num_sms, d->metric_id,
                                 d->integrator_id, d->precision, d->rlog ? 1 : 0, decide64, region,

@@ -68,6 +68,10 @@ extern "C" {
  * except within 2^-48 (relative) of a threshold. */
 #define FOORT_MIXED_FP64_DECISIONS 0x1u    /* take them in FP64 on the exact double value  */
 #define FOORT_MIXED_FP64_NEAR_HORIZON 0x2u /* whole steps in FP64 inside r_+ + margin       */
+/* whole steps in FP64 near turning points of r and theta: where |dr/dlambda| is below
+ * 5 % of r times the angular speed |u^theta| + |sin(theta) u^phi|, or |u^theta| below 5 %
+ * of |sin(theta) u^phi| */
+#define FOORT_MIXED_FP64_TURNING_POINTS 0x4u
 
 /* TermBitflag, Terminations.h:29-33 */
 #define FOORT_TERM_BOUNDARY_SPHERE 0x1u
@@ -330,7 +334,8 @@ int foort_gpu_launch_shape(foort_ctx* ctx, uint64_t n, foort_launch_shape* shape
 
 /* The launch-shape cache: one table per process, shared by every context. A key names
  * the GPU's SM count, the kernel variant (metric, integrator, precision, log-r, FP64
- * decisions, strong-field FP64 region) and the size bucket floor(log2 n) of the launch.
+ * decisions, FP64 steps by radius or at turning points) and the size bucket
+ * floor(log2 n) of the launch.
  * save / load write and read one text line per entry (load adds to the table). */
 uint32_t foort_tune_bucket(uint64_t n);
 int foort_tune_key(const foort_run_desc* desc, int32_t num_sms, uint64_t n, char* buf, uint64_t cap);

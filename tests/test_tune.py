@@ -31,6 +31,8 @@ def test_keys_name_the_kernel_variant_and_the_bucket():
     d.mixed_options = abi.MIXED_FP64_NEAR_HORIZON
     d.mixed_fp64_margin = 2.0
     assert fg.tune_key(d, 152, 3000).endswith(":f1:b11")
+    d.mixed_options = abi.MIXED_FP64_TURNING_POINTS
+    assert fg.tune_key(d, 152, 3000).endswith(":f2:b11")
     d4 = workloads.c4(abi.PREC_MIXED).desc
     assert fg.tune_key(d4, 152, 1 << 20) == "sm152:m3:i1:p1:r0:d0:f0:b20"
 
