@@ -17,6 +17,9 @@ LIB_PATH = os.path.join(HERE, "libfoort_gpu.so")
 
 _LIB = None
 
+# foort_dmesh_round_fn: (user, d_px, d_res, n, round) -> int
+DMESH_ROUND_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32)
+
 
 class FoortError(RuntimeError):
     def __init__(self, code, msg):
@@ -101,6 +104,22 @@ def load():
     lib.foort_tune_clear.restype = None
     lib.foort_tune_save.argtypes = [C.c_char_p]
     lib.foort_tune_load.argtypes = [C.c_char_p]
+    lib.foort_dmesh_create_v2.argtypes = [u64, u64, i32, u64, i32, u32, u32, u32, u32, vp, C.POINTER(vp)]
+    lib.foort_dmesh_is_finished.argtypes = [vp]
+    for f in ("cur_nr_geodesics", "grid", "rounds", "active"):
+        getattr(lib, "foort_dmesh_" + f).argtypes = [vp]
+        getattr(lib, "foort_dmesh_" + f).restype = u64
+    lib.foort_dmesh_pixels.argtypes = [vp]
+    lib.foort_dmesh_pixels.restype = vp
+    lib.foort_dmesh_get_pixels.argtypes = [vp, vp]
+    lib.foort_dmesh_set_results.argtypes = [vp, vp, u64]
+    lib.foort_dmesh_set_values.argtypes = [vp, vp, u64]
+    lib.foort_dmesh_end_current_loop.argtypes = [vp]
+    lib.foort_dmesh_last_error.argtypes = [vp]
+    lib.foort_dmesh_last_error.restype = C.c_char_p
+    lib.foort_dmesh_destroy.argtypes = [vp]
+    lib.foort_dmesh_destroy.restype = None
+    lib.foort_gpu_run_dmesh.argtypes = [vp, vp, vp, u64, DMESH_ROUND_FN, vp, C.POINTER(u64), C.POINTER(u32)]
     _LIB = lib
     return lib
 
@@ -371,6 +390,103 @@ class Mesh:
     def close(self):
         if self._m:
             self._lib.foort_mesh_destroy(self._m)
+            self._m = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceMesh:
+    """SquareSubdivisionMeshV2 held in device memory (include/foort_gpu.h foort_dmesh_*).
+    order: abi.DMESH_ORDER_REFERENCE (the reference's pixel order) or
+    abi.DMESH_ORDER_DEVICE. stream: a cudaStream_t as int (0 = legacy)."""
+
+    def __init__(self, diag_flags, value_diag, max_pixels=0, initial_pixels=0, max_subdivide=1,
+                 iteration_pixels=0, initial_sub_to_final=0, image=0, order=abi.DMESH_ORDER_REFERENCE, stream=0):
+        self._lib = load()
+        self._m = C.c_void_p()
+        rc = self._lib.foort_dmesh_create_v2(max_pixels, initial_pixels, max_subdivide, iteration_pixels,
+                                             initial_sub_to_final, diag_flags, value_diag, image, order,
+                                             C.c_void_p(stream), C.byref(self._m))
+        if rc != 0:
+            raise FoortError(rc, "device mesh creation failed")
+
+    @classmethod
+    def from_spec(cls, spec, diag_flags, value_diag, **kw):
+        kind, args = spec
+        if kind != "v2":
+            raise FoortError(abi.FOORT_E_UNSUPPORTED, "the device mesh is SquareSubdivisionMeshV2")
+        return cls(diag_flags, value_diag, **args, **kw)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise FoortError(rc, f"{what}: {self._lib.foort_dmesh_last_error(self._m).decode()}")
+
+    def finished(self):
+        return bool(self._lib.foort_dmesh_is_finished(self._m))
+
+    def size(self):
+        return self._lib.foort_dmesh_cur_nr_geodesics(self._m)
+
+    def grid(self):
+        return self._lib.foort_dmesh_grid(self._m)
+
+    def rounds(self):
+        return self._lib.foort_dmesh_rounds(self._m)
+
+    def active(self):
+        return self._lib.foort_dmesh_active(self._m)
+
+    def pixels_ptr(self):
+        """Device address of the round's pixels."""
+        return self._lib.foort_dmesh_pixels(self._m) or 0
+
+    def pixels(self):
+        """The round's pixels copied to the host."""
+        out = np.zeros(self.size(), dtype=abi.PIXEL_DTYPE)
+        self._check(self._lib.foort_dmesh_get_pixels(self._m, out.ctypes.data if len(out) else None), "get_pixels")
+        return out
+
+    def set_results_ptr(self, d_res, n):
+        self._check(self._lib.foort_dmesh_set_results(self._m, C.c_void_p(d_res), n), "set_results")
+
+    def set_values_ptr(self, d_values, n):
+        """n doubles in device memory, one per pixel of the round."""
+        self._check(self._lib.foort_dmesh_set_values(self._m, C.c_void_p(d_values), n), "set_values")
+
+    def end_round(self):
+        self._check(self._lib.foort_dmesh_end_current_loop(self._m), "end_current_loop")
+
+    def run(self, engine, d_out, cap_out, on_round=None):
+        """foort_gpu_run_dmesh with `engine`; on_round(d_px, d_res, n, round) is called
+        after each round's integration. Returns (geodesics, rounds)."""
+        err = []
+
+        def cb(_user, d_px, d_res, n, rnd):
+            try:
+                on_round(d_px or 0, d_res or 0, n, rnd)
+                return 0
+            except Exception as e:  # noqa: BLE001 -- reported after the run
+                err.append(e)
+                return abi.FOORT_E_BADARG
+
+        fn = DMESH_ROUND_FN(cb) if on_round else C.cast(None, DMESH_ROUND_FN)
+        g, r = C.c_uint64(), C.c_uint32()
+        rc = self._lib.foort_gpu_run_dmesh(engine._ctx, self._m, C.c_void_p(d_out), cap_out, fn, None, C.byref(g),
+                                           C.byref(r))
+        if err:
+            raise err[0]
+        if rc != 0:
+            msg = self._lib.foort_dmesh_last_error(self._m).decode() or engine.last_error()
+            raise FoortError(rc, f"run_dmesh: {msg}")
+        return g.value, r.value
+
+    def close(self):
+        if self._m:
+            self._lib.foort_dmesh_destroy(self._m)
             self._m = C.c_void_p()
 
     def __del__(self):

@@ -31,6 +31,11 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_FP64_ANALYTIC = 2  # every step in FP64 with the mixed kernel's analytic derivatives
 
+# device-resident mesh: order of the active squares (include/foort_gpu.h)
+DMESH_ORDER_REFERENCE = 0
+DMESH_ORDER_DEVICE = 1
+DMESH_MAX_CELLS = 1 << 29
+
 MIXED_FP64_DECISIONS = 0x1
 MIXED_FP64_NEAR_HORIZON = 0x2
 MIXED_FP64_TURNING_POINTS = 0x4

@@ -425,6 +425,67 @@ void foort_mesh_destroy(foort_mesh* mesh);
 /* The mesh's Mesh::getFullDescriptionStr() (Mesh.cpp:69-73, 697-707) into buf. */
 int foort_mesh_description(const foort_mesh* mesh, char* buf, uint64_t cap);
 
+/* ---- device-resident adaptive mesh ----------------------------------------------------
+ * SquareSubdivisionMeshV2 (Mesh.h:285-423, Mesh.cpp:660-1186) with its grid, values and
+ * pixel lists in DEVICE memory: a round's pixels go from the mesh to
+ * foort_gpu_integrate_async and the results back to the mesh without a host copy.
+ * Engine extension: the reference's mesh is host code.
+ *
+ * Ordering of the active squares (EndCurrentLoop, Mesh.cpp:1137-1148; std::sort, which is
+ * not stable, by weight then level):
+ *   FOORT_DMESH_ORDER_REFERENCE  a host copy of the active list (24 bytes per square) is
+ *       sorted with libstdc++'s std::sort in the reference's sequence: every round hands
+ *       out the reference's pixels, in the reference's order. Per round the new squares
+ *       come to the host and the squares to subdivide go back.
+ *   FOORT_DMESH_ORDER_DEVICE  the list stays on the device and is sorted there with the
+ *       grid cell as the last key. The rounds agree with the reference's where no two
+ *       squares of equal weight and level fall on either side of the IterationPixels cut.
+ * All calls are stream-ordered on `cuda_stream` (a cudaStream_t, 0 = legacy); create and
+ * end_current_loop wait for it. The grid takes 16 bytes per cell (R^2 cells, R as
+ * foort_mesh_grid), at most FOORT_DMESH_MAX_CELLS cells. The value diagnostic may not be
+ * GeodesicPosition (FOORT_E_UNSUPPORTED). */
+typedef struct foort_dmesh foort_dmesh;
+#define FOORT_DMESH_ORDER_REFERENCE 0u
+#define FOORT_DMESH_ORDER_DEVICE 1u
+#define FOORT_DMESH_MAX_CELLS (1ull << 29)
+
+/* SquareSubdivisionMeshV2(maxPixels, initialPixels, maxSubdivide, iterationPixels,
+ * initialSubToFinal, valdiag) whose pixels belong to image `image` of the run. */
+int foort_dmesh_create_v2(uint64_t max_pixels, uint64_t initial_pixels, int32_t max_subdivide,
+                          uint64_t iteration_pixels, int32_t initial_sub_to_final, uint32_t diag_flags,
+                          uint32_t value_diag, uint32_t image, uint32_t order, void* cuda_stream,
+                          foort_dmesh** out);
+int foort_dmesh_is_finished(const foort_dmesh* mesh);
+uint64_t foort_dmesh_cur_nr_geodesics(const foort_dmesh* mesh);
+uint64_t foort_dmesh_grid(const foort_dmesh* mesh);
+uint64_t foort_dmesh_rounds(const foort_dmesh* mesh);
+/* Squares with a positive weight not yet subdivided. */
+uint64_t foort_dmesh_active(const foort_dmesh* mesh);
+/* The current round's pixels: a DEVICE array of foort_dmesh_cur_nr_geodesics entries,
+ * valid until the next foort_dmesh_end_current_loop. */
+const foort_pixel* foort_dmesh_pixels(const foort_dmesh* mesh);
+/* The same copied to HOST memory (out: foort_dmesh_cur_nr_geodesics entries). */
+int foort_dmesh_get_pixels(foort_dmesh* mesh, foort_pixel* out);
+/* The round's values from DEVICE results (Geodesic::getDiagnosticFinalValue,
+ * Geodesic.cpp:141-149), or directly as one DEVICE double per pixel. n must be the
+ * round's pixel count. */
+int foort_dmesh_set_results(foort_dmesh* mesh, const foort_result* d_res, uint64_t n);
+int foort_dmesh_set_values(foort_dmesh* mesh, const double* d_values, uint64_t n);
+/* Mesh::EndCurrentLoop: weights, ordering and subdivision of the next round. */
+int foort_dmesh_end_current_loop(foort_dmesh* mesh);
+const char* foort_dmesh_last_error(const foort_dmesh* mesh);
+void foort_dmesh_destroy(foort_dmesh* mesh);
+
+/* A whole run on one device mesh: the round loop of Main.cpp:313-419. Each round's
+ * pixels are integrated into the DEVICE buffer d_out (room for cap_out results), then
+ * on_round (may be NULL) sees the round's DEVICE pixels and results (its non-zero return
+ * ends the run with that code), then the mesh takes the results and ends the round.
+ * Optional geodesics / rounds receive the totals. */
+typedef int (*foort_dmesh_round_fn)(void* user, const foort_pixel* d_px, const foort_result* d_res, uint64_t n,
+                                    uint32_t round);
+int foort_gpu_run_dmesh(foort_ctx* ctx, foort_dmesh* mesh, foort_result* d_out, uint64_t cap_out,
+                        foort_dmesh_round_fn on_round, void* user, uint64_t* geodesics, uint32_t* rounds);
+
 /* ---- Output files (GeodesicOutputHandler, InputOutput.h:40-110) -------------------------
  * Writes a run's results as FOORT does, byte for byte: one file per diagnostic, named
  * prefix_[timestamp_]Name[_n].ext, each starting with the first-line description, then
