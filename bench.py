@@ -8,15 +8,22 @@ C2: Kerr a=0.99 seen at 60 deg, 12 M half-width screen, SquareSubdivisionMeshV2 
 128^2 seed, MaxSubdivide 3, seed round + 4 refinement rounds), next to the plain FP64
 kernel on the same pixels and the endpoint error between the two.
 
-One step = every round of the workload:
-  value  pixel lists of all rounds resident in HBM, one persistent-kernel launch per
-         round through foort_gpu_integrate_async on one stream; CUDA events on that
+One step = one whole run of the workload (every geodesic of its mesh once):
+  value  the run's launches with their pixel lists resident in HBM, one persistent-kernel
+         launch each through foort_gpu_integrate_async on one stream; CUDA events on that
          stream around each step; L2 flushed (256 MB write) between steps; the launch
-         shape of each round chosen by the engine's autotuner (foort_gpu_autotune) in
-         the first warm-up step;
-  e2e    the full run through the public C ABI from pinned host memory: host mesh ->
-         foort_gpu_integrate (H2D of the pixels, kernel, D2H of the results) ->
-         foort_mesh_set_results -> foort_mesh_end_current_loop, every round.
+         shape of each launch chosen by the engine's autotuner (foort_gpu_autotune) in
+         the first warm-up step. The launches are the schedule's (--schedule): the
+         meshes' level waves, one launch per subdivision level (foort_gpu_run's default;
+         C2: 3 launches for the reference's 5 rounds, the same 26,547 pixels), or one per
+         round;
+  e2e    the whole run through the public C ABI, foort_gpu_run: host meshes, H2D of each
+         launch's pixels, kernel, D2H of its results, and the meshes' rounds replayed in
+         the reference's order. e2e_per_round_api: the same run through the per-round
+         call from pinned host memory (host mesh -> foort_gpu_integrate ->
+         foort_mesh_set_results -> foort_mesh_end_current_loop, every round);
+         rounds_schedule: the device-resident leg with one launch per round;
+         device_mesh: the run through foort_gpu_run_dmesh (mesh on the GPU).
 Accuracy (N = 1): the plain FP64 kernel (the reference's finite differences) on the same
 rounds, timed for the speed-up; the FP64-analytic oracle (every step in FP64 with the
 mixed kernel's derivatives) on all pixels; per-pixel condition numbers from two shifted
@@ -148,15 +155,16 @@ def kind_of(wl):
     return m, i
 
 
-def adaptive_rounds(eng_mod, wl, results_out=None):
-    """The pixel list of every round of the workload (one run with the engine)."""
+def adaptive_rounds(eng_mod, wl, results_out=None, waves=False):
+    """The pixel list of every round of the workload (one run with the engine), or of
+    every level wave (waves=True)."""
     px_rounds = []
     with eng_mod.Engine(wl.desc) as e:
         def keep(px, res):
             px_rounds.append(px.copy())
             if results_out is not None:
                 results_out.append(res.copy())
-        eng_mod.run_rounds(wl.mesh, wl.desc, e.integrate, keep)
+        eng_mod.run_rounds(wl.mesh, wl.desc, e.integrate, keep, waves=waves)
     return px_rounds
 
 
@@ -252,10 +260,10 @@ def run_reference(args, rank):
 
 def run_sharded(args, rank, world, local):
     """--shard: ONE run of the workload split over the ranks (strong scaling). Every rank
-    holds the same mesh; each round, each rank integrates its contiguous slice through the
-    C ABI from host memory and the slices are gathered before the mesh ends the round
-    (foort_gb300.multirank.sharded_run). value = the run's geodesics / the slowest rank's
-    time per run."""
+    holds the same mesh; each launch of the schedule (a level wave, or a round), each rank
+    integrates its contiguous slice through the C ABI from host memory and the slices are
+    gathered before the mesh goes on (foort_gb300.multirank.sharded_run). value = the run's
+    geodesics / the slowest rank's time per run."""
     import torch
     import foort_gb300
     from foort_gb300 import abi, multirank
@@ -267,15 +275,20 @@ def run_sharded(args, rank, world, local):
     wl = workload(args.workload, abi.PREC_MIXED, args.iteration_pixels)
     with foort_gb300.Engine(wl.desc) as e:
         def one_run():
-            n = [0, 0]
+            n = [0, 0, 0]
 
             def count(px, res):
                 n[0] += len(px)
                 n[1] += 1
-            multirank.sharded_run(wl.mesh, wl.desc, e.integrate, rank, world, dist, on_round=count)
+
+            def integrate(px):
+                n[2] += 1
+                return e.integrate(px)
+            multirank.sharded_run(wl.mesh, wl.desc, integrate, rank, world, dist, on_round=count,
+                                  waves=args.schedule == "waves")
             return n
         for _ in range(args.warmup):
-            n_geod, n_rounds = one_run()
+            n_geod, n_rounds, n_launch = one_run()
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -295,7 +308,7 @@ def run_sharded(args, rank, world, local):
             "config": dict(config_block(wl, args, rounds=n_rounds, geod=n_geod), parallelism=f"shard{world}"),
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": n_geod * abi.PIXEL_DTYPE.itemsize,
                     "d2h_bytes_per_step": n_geod * abi.RESULT_DTYPE.itemsize},
-            "gpu_launches": args.steps * n_rounds}), flush=True)
+            "schedule": args.schedule, "gpu_launches": args.steps * n_launch}), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
@@ -390,6 +403,8 @@ def main():
     ap.add_argument("--shard", action="store_true",
                     help="one run split over the ranks, gathered each round (strong scaling) instead of one "
                          "independent run per rank")
+    ap.add_argument("--schedule", default="waves", choices=["waves", "rounds"],
+                    help="launches of a run: the meshes' level waves (foort_gpu_run's default) or one per round")
     ap.add_argument("--no-tune", action="store_true",
                     help="use the built-in launch rule instead of autotuning each round in the first warm-up step")
     ap.add_argument("--cpu-seconds", type=float, default=None,
@@ -427,39 +442,65 @@ def main():
     def max_over_ranks(x):
         return multirank.max_over_ranks(x, dist, device="cuda")
 
-    # ---- prepare: the workload's pixel lists (one adaptive run with the mixed kernel)
+    # ---- prepare: the workload's pixel lists (one adaptive run with the mixed kernel): the
+    # reference's rounds, and the launches of the schedule (the level waves: one launch per
+    # subdivision level, the same pixels; or the rounds themselves)
     wl = workload(args.workload, abi.PREC_MIXED, args.iteration_pixels)
     mkind = kind_of(wl)
     t0 = time.perf_counter()
-    prep_results = []
-    rounds = adaptive_rounds(foort_gb300, wl, prep_results)
-    log(f"[bench] {wl.name}: {len(rounds)} rounds, sizes {[len(r) for r in rounds]}, prepare {time.perf_counter() - t0:.1f}s")
+    rounds = adaptive_rounds(foort_gb300, wl)
+    launches_px = adaptive_rounds(foort_gb300, wl, waves=True) if args.schedule == "waves" else rounds
+    log(f"[bench] {wl.name}: {len(rounds)} rounds, sizes {[len(r) for r in rounds]}; {args.schedule}: "
+        f"{[len(r) for r in launches_px]}; prepare {time.perf_counter() - t0:.1f}s")
     n_geod = sum(len(r) for r in rounds)
+    assert sum(len(r) for r in launches_px) == n_geod
     stream = torch.cuda.Stream()
-    d_px = [torch.from_numpy(r.view(np.uint8)).to("cuda") for r in rounds]
-    d_out = [torch.empty(len(r) * abi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda") for r in rounds]
+
+    def to_device(lists):
+        return ([torch.from_numpy(r.view(np.uint8)).to("cuda") for r in lists],
+                [torch.empty(len(r) * abi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda") for r in lists])
+
+    d_px, d_out = to_device(launches_px)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
-    rhs_per_round = [0] * len(rounds)
-    lanes_per_round = [1] * len(rounds)
-    shapes = [None] * len(rounds)
+    rhs_per_round = [0] * len(launches_px)
+    lanes_per_round = [1] * len(launches_px)
+    shapes = [None] * len(launches_px)
 
-    def device_step(e, tune=False):
+    def device_step(e, tune=False, lists=None):
         kms = []
+        dpx, dout, lst = lists if lists else (d_px, d_out, launches_px)
         with torch.cuda.stream(stream):
-            for i, (dp, do, r) in enumerate(zip(d_px, d_out, rounds)):
+            for i, (dp, do, r) in enumerate(zip(dpx, dout, lst)):
                 if tune:  # the project autotuner: search, cache, and integrate in the best shape
                     e.autotune(dp.data_ptr(), len(r), do.data_ptr(), stream.cuda_stream)
                 else:
                     e.integrate_async(dp.data_ptr(), len(r), do.data_ptr(), stream.cuda_stream)
                     e.sync()
                 st = e.stats()
+                kms.append(st["kernel_ms"])
+                if lists:
+                    continue
                 shapes[i] = {"geodesics": len(r), "block_size": st["block_size"], "lanes": st["lanes_per_geodesic"],
                              "refill_steps": st["refill_steps"], "poll_steps": st["poll_steps"]}
-                kms.append(st["kernel_ms"])
                 rhs_per_round[i] = st["rhs_evals"]
                 lanes_per_round[i] = st["lanes_per_geodesic"]
         return kms
+
+    def timed_steps(e, lists=None):
+        ms, kms_all = [], []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            kms = device_step(e, lists=lists)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+            kms_all.extend(kms)
+        return ms, kms_all
 
     # ---- value: device-resident inputs
     peaks = foort_gb300.measure_peaks()
@@ -475,18 +516,7 @@ def main():
         tuned_shapes = [dict(sh) for sh in shapes]  # the FP64 leg reuses device_step
         clocks = ClockSampler(local)
         clocks.start()
-        step_ms, launch_ms, steps_per_launch = [], [], []
-        for _ in range(args.steps):
-            flush.fill_(1)
-            torch.cuda.synchronize()
-            ev0 = torch.cuda.Event(enable_timing=True)
-            ev1 = torch.cuda.Event(enable_timing=True)
-            ev0.record(stream)
-            kms = device_step(e)
-            ev1.record(stream)
-            ev1.synchronize()
-            step_ms.append(ev0.elapsed_time(ev1))
-            launch_ms.extend(kms)
+        step_ms, launch_ms = timed_steps(e)
         barrier()
         clk = clocks.stop()
         mixed_res = [np.frombuffer(do.cpu().numpy().tobytes(), dtype=abi.RESULT_DTYPE) for do in d_out]
@@ -495,7 +525,64 @@ def main():
     value = world * n_geod / (t_step * 1e-3)
     steps_total = sum(int(r["steps"].sum()) for r in mixed_res)
 
-    # ---- e2e: public C ABI from pinned host memory, host mesh in the loop
+    # ---- the same pixels launched round by round (the reference's rounds), device-resident;
+    # sizes the search has not seen are tuned in the warm-up
+    rounds_leg = None
+    if launches_px is not rounds:
+        r_lists = to_device(rounds) + (rounds,)
+        with foort_gb300.Engine(wl.desc) as e:
+            e.set_lanes(args.lanes)
+            e.set_autotune(not args.no_tune)
+            for _ in range(args.warmup):
+                device_step(e, lists=r_lists)
+            barrier()
+            r_ms, _ = timed_steps(e, lists=r_lists)
+            barrier()
+        t_r = max_over_ranks(sum(r_ms) / len(r_ms))
+        rounds_leg = {"value": world * n_geod / (t_r * 1e-3), "unit": UNIT, "ms_per_step": t_r,
+                      "launches_per_step": len(rounds),
+                      "scope": "the same pixels, one launch per round of the reference's mesh, device-resident"}
+        del r_lists
+
+    # ---- e2e: a whole run through the public C ABI (foort_gpu_run: host mesh, H2D of each
+    # launch's pixels, kernel, D2H of its results, mesh rounds), and the same run through
+    # the per-round call (foort_gpu_integrate from pinned host memory, round after round:
+    # what a binding inside the reference's own round loop does)
+    def new_meshes():
+        return [foort_gb300.Mesh.from_spec(spec, wl.desc.diag_flags, wl.desc.value_diag) for spec in wl.mesh]
+
+    run_launches = []
+
+    def e2e_run(e):
+        meshes = new_meshes()
+        try:
+            g, _ = e.run(meshes)
+        finally:
+            for m in meshes:
+                m.close()
+        assert g == n_geod
+        run_launches.append(e.run_info())
+
+    with foort_gb300.Engine(wl.desc) as e:
+        e.set_lanes(args.lanes)
+        e.set_schedule(abi.SCHEDULE_WAVES if args.schedule == "waves" else abi.SCHEDULE_ROUNDS)
+        for _ in range(args.warmup):
+            e2e_run(e)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_run(e)
+        barrier()
+        t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    n_launch_run, sched_used = run_launches[-1]
+    # every pixel goes up once and its result comes back once when the launches are the
+    # schedule's (no pixel integrated twice)
+    assert n_launch_run == len(launches_px), (n_launch_run, len(launches_px))
+    e2e = {"value": world * n_geod / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n_geod * abi.PIXEL_DTYPE.itemsize,
+           "d2h_bytes_per_step": n_geod * abi.RESULT_DTYPE.itemsize, "ms_per_step": t_e2e * 1e3,
+           "api": "foort_gpu_run", "launches_per_step": n_launch_run,
+           "schedule": "level waves" if sched_used == abi.SCHEDULE_WAVES else "rounds"}
+
     h2d = d2h = 0
     pin_px = [torch.empty(len(r) * abi.PIXEL_DTYPE.itemsize, dtype=torch.uint8).pin_memory() for r in rounds]
     pin_out = [torch.empty(len(r) * abi.RESULT_DTYPE.itemsize, dtype=torch.uint8).pin_memory() for r in rounds]
@@ -532,9 +619,40 @@ def main():
         for _ in range(args.steps):
             e2e_step(e)
         barrier()
-        t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps)
-    e2e = {"value": world * n_geod / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-           "ms_per_step": t_e2e * 1e3}
+        t_e2e_r = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    e2e_rounds = {"value": world * n_geod / t_e2e_r, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                  "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e_r * 1e3, "api": "foort_gpu_integrate per round",
+                  "launches_per_step": len(rounds)}
+
+    # ---- device-resident mesh: the same run through foort_gpu_run_dmesh, mesh state and
+    # results in device memory (one V2 mesh). The warm-up run checks every round's pixels
+    # against the host mesh's.
+    dmesh = None
+    if len(wl.mesh) == 1 and wl.mesh[0][0] == "v2":
+        cap = max(len(r) for r in rounds)
+        d_res = torch.empty(cap * abi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        same = []
+
+        def new_mesh():
+            return foort_gb300.DeviceMesh.from_spec(wl.mesh[0], wl.desc.diag_flags, wl.desc.value_diag)
+
+        with foort_gb300.Engine(wl.desc) as e:
+            e.set_lanes(args.lanes)
+            dm = new_mesh()
+            g_dm, r_dm = dm.run(e, d_res.data_ptr(), cap, lambda d_px, d_r, n, k: same.append(
+                k < len(rounds) and np.array_equal(dm.pixels(), rounds[k])))
+            dm.close()
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                dm = new_mesh()
+                dm.run(e, d_res.data_ptr(), cap)
+                dm.close()
+            barrier()
+            t_dm = max_over_ranks((time.perf_counter() - t0) / args.steps)
+        dmesh = {"value": world * n_geod / t_dm, "unit": UNIT, "ms_per_step": t_dm * 1e3, "geodesics": g_dm,
+                 "rounds": r_dm, "same_pixels_as_host_mesh": len(same) == len(rounds) and all(same),
+                 "scope": "whole run, device-resident V2 mesh (reference order), results left in device memory"}
 
     # ---- FP64 plain kernel on the same pixels (N = 1 only: under torchrun the other GPUs
     # would wait for it)
@@ -559,12 +677,12 @@ def main():
                 "roofline_fp64": {"achieved": steps64 * OPS_PER_STEP.get(mkind, 1130) / (t64 * 1e-3) / 1e12,
                                   "peak": peaks[1], "unit": "TFLOP/s",
                                   "frac": steps64 * OPS_PER_STEP.get(mkind, 1130) / (t64 * 1e-3) / 1e12 / peaks[1]}}
-        acc = accuracy_legs(foort_gb300, args, wl, np.concatenate(rounds), np.concatenate(mixed_res),
+        acc = accuracy_legs(foort_gb300, args, wl, np.concatenate(launches_px), np.concatenate(mixed_res),
                             np.concatenate(res64))
 
     # ---- roofline of the dominant kernel: the mixed kernel over all launches of a step
     # (each round is one launch of it), and its largest launch alone
-    n_launch = len(rounds)
+    n_launch = len(launches_px)
     per_launch_ms = [launch_ms[i::n_launch] for i in range(n_launch)]
     ops = OPS_PER_STEP.get(mkind, 1130)
 
@@ -578,7 +696,7 @@ def main():
     tot_ops = sum(launch_ops(i)[0] for i in range(n_launch))
     tot_ms = sum(statistics.mean(m) for m in per_launch_ms)
     achieved = tot_ops / (tot_ms * 1e-3) / 1e12
-    big = int(np.argmax([len(r) for r in rounds]))
+    big = int(np.argmax([len(r) for r in launches_px]))
     big_ms = statistics.mean(per_launch_ms[big])
     big_ops, big_steps = launch_ops(big)
     # executed instructions: the issue-slot fraction of the whole step
@@ -590,7 +708,7 @@ def main():
     # DRAM bytes (read + write) of one launch, from ncu's per-geodesic figure scaled to the
     # launch's geodesics (the capture is a 6,000-geodesic sample of the same grid)
     tpg = DRAM_BYTES_PER_GEODESIC.get(mkind)
-    traffic = tpg * len(rounds[big]) if tpg else None
+    traffic = tpg * len(launches_px[big]) if tpg else None
     roofline = {"bound": "alu-fp32", "achieved": achieved, "peak": peaks[0], "unit": "TFLOP/s",
                 "frac": achieved / peaks[0], "traffic": traffic, "traffic_unit": "bytes per launch (largest launch)",
                 "scope": f"all {n_launch} launches of a step: {tot_ops:.4g} reference-formulation operations in "
@@ -600,7 +718,7 @@ def main():
                                "has no FP32/FP64 entry",
                 "kernel": "integrate_mixed_pair_kernel" if mixed_lanes[big] == 2 else "integrate_mixed_kernel",
                 "lanes_per_geodesic": mixed_lanes,
-                "largest_launch": {"geodesics": len(rounds[big]), "launch_ms": big_ms, "steps": big_steps,
+                "largest_launch": {"geodesics": len(launches_px[big]), "launch_ms": big_ms, "steps": big_steps,
                                    "achieved": big_ops / (big_ms * 1e-3) / 1e12,
                                    "frac": big_ops / (big_ms * 1e-3) / 1e12 / peaks[0]},
                 "executed": {"thread_instructions_per_step": {f"{k[2]}-lane": v for k, v in EXEC_INSTR_PER_STEP.items()
@@ -626,13 +744,17 @@ def main():
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "mixed-f32 (FP32 right-hand side; float-float state and decisions)", "data": "synthetic",
         "config": dict(config_block(wl, args, rounds=len(rounds), geod=n_geod),
+                       schedule=("level waves: one launch per subdivision level, the reference's rounds replayed "
+                                 "from their results" if launches_px is not rounds else "one launch per round"),
                        autotuned=not args.no_tune, launch_shapes=tuned_shapes),
         "geodesics_per_step": world * n_geod, "steps_per_s": world * steps_total / (t_step * 1e-3),
-        "gpu_launches": args.steps * len(rounds),
-        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+        "gpu_launches": args.steps * len(launches_px),
+        "e2e": e2e, "e2e_per_round_api": e2e_rounds, "rounds_schedule": rounds_leg, "device_mesh": dmesh,
+        "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "fp64": fp64, "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
         "accuracy": acc,
         "round_sizes": [len(r) for r in rounds],
+        "launch_sizes": [len(r) for r in launches_px],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

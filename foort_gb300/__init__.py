@@ -104,6 +104,9 @@ def load():
     lib.foort_tune_clear.restype = None
     lib.foort_tune_save.argtypes = [C.c_char_p]
     lib.foort_tune_load.argtypes = [C.c_char_p]
+    lib.foort_mesh_create_waves.argtypes = [vp, C.POINTER(vp)]
+    lib.foort_gpu_set_schedule.argtypes = [vp, u32]
+    lib.foort_gpu_run_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u32)]
     lib.foort_dmesh_create_v2.argtypes = [u64, u64, i32, u64, i32, u32, u32, u32, u32, vp, C.POINTER(vp)]
     lib.foort_dmesh_is_finished.argtypes = [vp]
     for f in ("cur_nr_geodesics", "grid", "rounds", "active"):
@@ -244,6 +247,16 @@ class Engine:
         self._check(self._lib.foort_gpu_run(self._ctx, ms, os_, n, C.byref(g), C.byref(r)))
         return g.value, r.value
 
+    def set_schedule(self, schedule=abi.SCHEDULE_WAVES):
+        """foort_gpu_run's launches: level waves where they apply, or one per round."""
+        self._check(self._lib.foort_gpu_set_schedule(self._ctx, schedule))
+
+    def run_info(self):
+        """(launches, schedule) of the last foort_gpu_run."""
+        n, sch = C.c_uint32(), C.c_uint32()
+        self._check(self._lib.foort_gpu_run_info(self._ctx, C.byref(n), C.byref(sch)))
+        return n.value, sch.value
+
     def stats(self):
         s = abi.Stats()
         self._lib.foort_gpu_get_stats(self._ctx, C.byref(s))
@@ -372,6 +385,16 @@ class Mesh:
 
     def end_round(self):
         self._lib.foort_mesh_end_current_loop(self._m)
+
+    def waves(self):
+        """The mesh's level waves (foort_mesh_create_waves) as a new Mesh."""
+        w = Mesh.__new__(Mesh)
+        w._lib = self._lib
+        w._m = C.c_void_p()
+        rc = self._lib.foort_mesh_create_waves(self._m, C.byref(w._m))
+        if rc != 0:
+            raise FoortError(rc, "this mesh has no level waves")
+        return w
 
     def description(self):
         buf = C.create_string_buffer(1024)
@@ -579,12 +602,18 @@ def config_mesh(cfg):
     return m
 
 
-def run_rounds(mesh_specs, desc, integrate, on_round=None):
+def run_rounds(mesh_specs, desc, integrate, on_round=None, waves=False):
     """One FOORT run (the round loop of Main.cpp:313-419) over one mesh per image, the
     images' meshes advancing in lockstep so that each round is one integrate() call over
     the pixels of every unfinished image. mesh_specs: Mesh.from_spec specs; integrate(px)
-    -> results; on_round(px, res) after each round. Returns the number of rounds."""
+    -> results; on_round(px, res) after each round. waves: the meshes' level waves
+    (Mesh.waves) instead of their rounds. Returns the number of rounds."""
     meshes = [Mesh.from_spec(spec, desc.diag_flags, desc.value_diag) for spec in mesh_specs]
+    if waves:
+        base, meshes = meshes, []
+        for m in base:
+            meshes.append(m.waves())
+            m.close()
     n_rounds = 0
     try:
         while True:
@@ -606,6 +635,46 @@ def run_rounds(mesh_specs, desc, integrate, on_round=None):
         for m in meshes:
             m.close()
     return n_rounds
+
+
+def _pixel_keys(px):
+    return (px["image"].astype(np.int64) << 42) | (px["row"].astype(np.int64) * px["grid"].astype(np.int64)
+                                                 + px["col"].astype(np.int64))
+
+
+def run_by_waves(mesh_specs, desc, integrate, on_round=None):
+    """foort_gpu_run's level-wave schedule with any integrate(px) -> results: the meshes'
+    level waves (Mesh.waves) are integrated first, one integrate() call per wave, then the
+    meshes' rounds are replayed from the stored results, so on_round(px, res) sees the
+    reference's rounds. A round's pixels that no wave held (none, for meshes that have
+    waves) go to integrate() then. Returns (rounds, integrate calls)."""
+    keys, results = [], []
+
+    def wave(px):
+        res = integrate(px)
+        keys.append(_pixel_keys(px))
+        results.append(res)
+        return res
+
+    calls = run_rounds(mesh_specs, desc, wave, waves=True)
+    k = np.concatenate(keys) if keys else np.zeros(0, np.int64)
+    r = np.concatenate(results) if results else np.zeros(0, abi.RESULT_DTYPE)
+    order = np.argsort(k, kind="stable")
+    k, r = k[order], r[order]
+    extra = [0]
+
+    def lookup(px):
+        q = _pixel_keys(px)
+        i = np.minimum(np.searchsorted(k, q), max(len(k) - 1, 0))
+        found = (k[i] == q) if len(k) else np.zeros(len(q), bool)
+        res = r[i].copy() if len(k) else np.zeros(len(q), abi.RESULT_DTYPE)
+        if not found.all():
+            res[~found] = integrate(px[~found])
+            extra[0] += 1
+        return res
+
+    rounds = run_rounds(mesh_specs, desc, lookup, on_round)
+    return rounds, calls + extra[0]
 
 
 def run_config(path, precision=abi.PREC_MIXED, output_dir=None):

@@ -31,6 +31,10 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_FP64_ANALYTIC = 2  # every step in FP64 with the mixed kernel's analytic derivatives
 
+# foort_gpu_run's schedule (include/foort_gpu.h)
+SCHEDULE_WAVES = 0
+SCHEDULE_ROUNDS = 1
+
 # device-resident mesh: order of the active squares (include/foort_gpu.h)
 DMESH_ORDER_REFERENCE = 0
 DMESH_ORDER_DEVICE = 1

@@ -41,6 +41,8 @@ struct foort_ctx {
     int device = 0, num_sms = 0;
     bool pending = false;
     bool autotune = false;  // search shapes for launches without a cache entry
+    uint32_t schedule = FOORT_SCHEDULE_WAVES;  // foort_gpu_run
+    uint32_t run_launches = 0, run_schedule = 0;
     foort_stats stats{};
     std::string err;
 };
@@ -690,6 +692,27 @@ int foort_gpu_launch_shape(foort_ctx* ctx, uint64_t n, foort_launch_shape* shape
     if (rc) return rc;
     *shape = foort_launch_shape{ls.block, want.blocks_per_sm, ls.lanes, ls.refill, ls.poll, 0, want.ms};
     return FOORT_OK;
+}
+
+int foort_gpu_set_schedule(foort_ctx* ctx, uint32_t schedule) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    if (schedule > FOORT_SCHEDULE_ROUNDS) return fail(ctx, FOORT_E_BADARG, "unknown schedule");
+    ctx->schedule = schedule;
+    return FOORT_OK;
+}
+
+int foort_gpu_run_info(const foort_ctx* ctx, uint32_t* launches, uint32_t* schedule) {
+    if (!ctx) return FOORT_E_BADARG;
+    if (launches) *launches = ctx->run_launches;
+    if (schedule) *schedule = ctx->run_schedule;
+    return FOORT_OK;
+}
+
+uint32_t foort_ctx_schedule(const foort_ctx* ctx) { return ctx->schedule; }
+uint64_t foort_ctx_budget(const foort_ctx* ctx) { return ctx->budget; }
+void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule) {
+    ctx->run_launches = launches;
+    ctx->run_schedule = schedule;
 }
 
 int foort_gpu_get_desc(const foort_ctx* ctx, foort_run_desc* desc) {

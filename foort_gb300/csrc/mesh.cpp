@@ -64,6 +64,9 @@ struct foort_mesh {
     virtual bool done() const = 0;
     virtual uint64_t rounds() const = 0;
     virtual std::string description() const = 0;  // Mesh::getFullDescriptionStr
+    // The same mesh, unstarted, with every square of positive weight subdivided in each
+    // round (foort_mesh_create_waves); null where that is not this mesh's pixel set.
+    virtual foort_mesh* wave_clone() const = 0;
 };
 
 namespace {
@@ -84,6 +87,12 @@ struct SimpleMesh final : foort_mesh {
     // Mesh.cpp:69-73
     std::string description() const override {
         return "Mesh: simple square grid (" + std::to_string(grid) + "^2 pixels)";
+    }
+    foort_mesh* wave_clone() const override {
+        if (fin) return nullptr;
+        auto* m = new SimpleMesh(*this);
+        m->err.clear();
+        return m;
     }
 };
 
@@ -234,6 +243,26 @@ struct V2Mesh final : foort_mesh {
                "; row/column size: " + std::to_string(grid) + ")";
     }
 
+    // With unlimited MaxPixels the reference's rounds continue until no square of
+    // positive weight is left, so every such square is subdivided in some round: the
+    // run's pixel set is fixed by the values alone, and IterationPixels only spreads it
+    // over rounds. With IterationPixels unlimited, round k hands out the pixels of
+    // subdivision level k.
+    foort_mesh* wave_clone() const override {
+        if (!infinite || n_rounds != 0) return nullptr;
+        auto* m = new V2Mesh();
+        m->kind = kind;
+        m->grid = grid;
+        m->diag_flags = diag_flags;
+        m->value_diag = value_diag;
+        m->initial = initial;
+        m->max_sub = max_sub;
+        m->iteration = UINT64_MAX;
+        m->sub_to_final = sub_to_final;
+        m->init_grid();
+        return m;
+    }
+
     // EndCurrentLoop, Mesh.cpp:1092-1186
     void end_loop() override {
         ++n_rounds;
@@ -345,6 +374,12 @@ int foort_mesh_end_current_loop(foort_mesh* m) {
 }
 
 void foort_mesh_destroy(foort_mesh* m) { delete m; }
+
+int foort_mesh_create_waves(const foort_mesh* m, foort_mesh** out) {
+    if (!m || !out) return FOORT_E_BADARG;
+    *out = m->wave_clone();
+    return *out ? FOORT_OK : FOORT_E_UNSUPPORTED;
+}
 
 int foort_mesh_description(const foort_mesh* m, char* buf, uint64_t cap) {
     if (!m || !buf || cap == 0) return FOORT_E_BADARG;

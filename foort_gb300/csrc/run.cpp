@@ -7,49 +7,165 @@
 // (GeodesicFinished, Main.cpp:399) and to each image's output files
 // (NewGeodesicOutput, Main.cpp:400); then each mesh ends its round (EndCurrentLoop,
 // Main.cpp:410). Images advance in lockstep, so a round is one launch over all images.
+//
+// Level waves (FOORT_SCHEDULE_WAVES). A launch lasts as long as its slowest geodesic, and
+// on the adaptive mesh's rounds that is most of the launch: C2's geodesics all take
+// 66,000-71,000 steps, so a round of 1,079 geodesics takes as long as one of 16,384. With
+// unlimited MaxPixels the mesh's pixel set is fixed by the values alone
+// (foort_mesh_create_waves), and it splits into one wave per subdivision level, each
+// depending only on the results of the waves before. The run integrates the waves first
+// (C2: three launches where the reference has five rounds), then replays the meshes'
+// rounds from the stored results, so meshes and output files see the reference's rounds.
 #include <algorithm>
 #include <cstring>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/foort_gpu.h"
 #include "diag_order.h"
 
-extern "C" int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs,
-                             uint32_t n_images, uint64_t* geodesics, uint32_t* rounds) {
-    if (!ctx || !meshes || n_images == 0) return FOORT_E_BADARG;
-    for (uint32_t i = 0; i < n_images; ++i)
-        if (!meshes[i]) return FOORT_E_BADARG;
-    foort_run_desc desc;
-    if (foort_gpu_get_desc(ctx, &desc)) return FOORT_E_BADARG;
-    const bool geopos = (desc.diag_flags & FOORT_DIAG_GEODESIC_POSITION) != 0;
-    const std::vector<uint32_t> order = foort::diagnostic_order(desc.diag_flags, desc.value_diag);
-    const uint32_t value_first = order.empty() ? 0u : order[0];
-    uint64_t total = 0;
-    uint32_t n_rounds = 0;
+// engine.cu (internal)
+extern "C" {
+uint32_t foort_ctx_schedule(const foort_ctx* ctx);
+uint64_t foort_ctx_budget(const foort_ctx* ctx);
+void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule);
+}
+
+namespace {
+
+// The pixels of every unfinished mesh, image after image; count[i] pixels of image i
+// (0 for a finished mesh). any: some mesh is unfinished.
+int gather(foort_mesh* const* meshes, uint32_t n_images, std::vector<foort_pixel>& px, std::vector<uint64_t>& count,
+           bool& any) {
+    uint64_t n = 0;
+    any = false;
+    for (uint32_t i = 0; i < n_images; ++i) {
+        const int fin = foort_mesh_is_finished(meshes[i]);
+        if (fin < 0) return fin;
+        count[i] = fin ? 0 : foort_mesh_cur_nr_geodesics(meshes[i]);
+        any = any || !fin;
+        n += count[i];
+    }
+    px.resize(n);
+    uint64_t k = 0;
+    for (uint32_t i = 0; i < n_images; ++i) {
+        if (foort_mesh_is_finished(meshes[i])) continue;
+        const int rc = foort_mesh_get_pixels(meshes[i], i, px.data() + k);
+        if (rc) return rc;
+        k += count[i];
+    }
+    return FOORT_OK;
+}
+
+// Results of integrated pixels by image and grid cell.
+struct ResultStore {
+    std::vector<std::unordered_map<uint64_t, uint64_t>> slot;  // per image: row * grid + col -> index in res
+    std::vector<foort_result> res;
+};
+
+uint64_t cell_of(const foort_pixel& p) { return p.row * p.grid + p.col; }
+
+// Integrate the meshes' level waves, one launch per wave over all images, and keep every
+// result. FOORT_E_UNSUPPORTED (nothing integrated) where a mesh has no waves.
+int integrate_waves(foort_ctx* ctx, foort_mesh* const* meshes, uint32_t n_images, ResultStore& store,
+                    uint32_t& launches) {
+    std::vector<foort_mesh*> waves(n_images, nullptr);
+    auto release = [&]() {
+        for (foort_mesh* w : waves) foort_mesh_destroy(w);
+    };
+    for (uint32_t i = 0; i < n_images; ++i) {
+        if (foort_mesh_create_waves(meshes[i], &waves[i]) != FOORT_OK) {
+            release();
+            return FOORT_E_UNSUPPORTED;
+        }
+    }
+    store.slot.assign(n_images, {});
     std::vector<foort_pixel> px;
     std::vector<foort_result> res;
     std::vector<uint64_t> count(n_images);
     int rc = FOORT_OK;
     for (;;) {
-        uint64_t n = 0;
-        for (uint32_t i = 0; i < n_images; ++i) {
-            const int fin = foort_mesh_is_finished(meshes[i]);
-            if (fin < 0) return fin;
-            count[i] = fin ? 0 : foort_mesh_cur_nr_geodesics(meshes[i]);
-            n += count[i];
-        }
         bool any = false;
-        for (uint32_t i = 0; i < n_images; ++i) any = any || foort_mesh_is_finished(meshes[i]) == 0;
-        if (!any) break;
-        px.resize(n);
-        res.resize(n);
+        if ((rc = gather(waves.data(), n_images, px, count, any)) || !any) break;
+        res.resize(px.size());
+        if ((rc = foort_gpu_integrate(ctx, px.data(), px.size(), res.data()))) break;
+        ++launches;
         uint64_t k = 0;
-        for (uint32_t i = 0; i < n_images; ++i) {
-            if (foort_mesh_is_finished(meshes[i])) continue;
-            if ((rc = foort_mesh_get_pixels(meshes[i], i, px.data() + k))) return rc;
+        for (uint32_t i = 0; i < n_images && rc == FOORT_OK; ++i) {
+            if (foort_mesh_is_finished(waves[i])) continue;
+            for (uint64_t g = k; g < k + count[i]; ++g) {
+                store.slot[i][cell_of(px[g])] = store.res.size();
+                store.res.push_back(res[g]);
+            }
+            rc = foort_mesh_set_results(waves[i], res.data() + k, count[i]);
+            if (!rc) rc = foort_mesh_end_current_loop(waves[i]);
             k += count[i];
         }
-        rc = foort_gpu_integrate(ctx, px.data(), n, res.data());
+        if (rc) break;
+    }
+    release();
+    return rc;
+}
+
+// The round's results from the store; the pixels it lacks are integrated in one launch.
+int results_from_store(foort_ctx* ctx, const ResultStore& store, const std::vector<foort_pixel>& px,
+                       std::vector<foort_result>& res, uint32_t& launches) {
+    std::vector<uint64_t> miss;
+    for (uint64_t g = 0; g < px.size(); ++g) {
+        const auto& m = store.slot[px[g].image];
+        const auto it = m.find(cell_of(px[g]));
+        if (it == m.end()) {
+            miss.push_back(g);
+        } else {
+            res[g] = store.res[it->second];
+        }
+    }
+    if (miss.empty()) return FOORT_OK;
+    std::vector<foort_pixel> mp(miss.size());
+    std::vector<foort_result> mr(miss.size());
+    for (uint64_t j = 0; j < miss.size(); ++j) mp[j] = px[miss[j]];
+    const int rc = foort_gpu_integrate(ctx, mp.data(), mp.size(), mr.data());
+    ++launches;
+    if (rc) return rc;
+    for (uint64_t j = 0; j < miss.size(); ++j) res[miss[j]] = mr[j];
+    return FOORT_OK;
+}
+
+int run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs, uint32_t n_images,
+        uint64_t* geodesics, uint32_t* rounds, uint32_t& launches, uint32_t& schedule) {
+    foort_run_desc desc;
+    if (foort_gpu_get_desc(ctx, &desc)) return FOORT_E_BADARG;
+    const bool geopos = (desc.diag_flags & FOORT_DIAG_GEODESIC_POSITION) != 0;
+    const std::vector<uint32_t> order = foort::diagnostic_order(desc.diag_flags, desc.value_diag);
+    const uint32_t value_first = order.empty() ? 0u : order[0];
+    int rc = FOORT_OK;
+    ResultStore store;
+    schedule = FOORT_SCHEDULE_ROUNDS;
+    if (foort_ctx_schedule(ctx) == FOORT_SCHEDULE_WAVES && !geopos && foort_ctx_budget(ctx) == 0) {
+        rc = integrate_waves(ctx, meshes, n_images, store, launches);
+        if (rc == FOORT_OK) {
+            schedule = FOORT_SCHEDULE_WAVES;
+        } else if (rc != FOORT_E_UNSUPPORTED) {
+            return rc;
+        }
+    }
+    uint64_t total = 0;
+    uint32_t n_rounds = 0;
+    std::vector<foort_pixel> px;
+    std::vector<foort_result> res;
+    std::vector<uint64_t> count(n_images);
+    for (;;) {
+        bool any = false;
+        if ((rc = gather(meshes, n_images, px, count, any))) return rc;
+        if (!any) break;
+        const uint64_t n = px.size();
+        res.resize(n);
+        if (schedule == FOORT_SCHEDULE_WAVES) {
+            rc = results_from_store(ctx, store, px, res, launches);
+        } else {
+            rc = foort_gpu_integrate(ctx, px.data(), n, res.data());
+            ++launches;
+        }
         if (rc != FOORT_OK) return rc;
         // GeodesicPosition: a second pass records the positions (foort_gpu_positions)
         std::vector<uint64_t> counts, first;
@@ -57,10 +173,12 @@ extern "C" int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_ou
         if (geopos) {
             counts.resize(n);
             first.resize(n);
-            uint64_t total = 0;
-            if ((rc = foort_gpu_positions(ctx, px.data(), n, res.data(), counts.data(), nullptr, 0, &total))) return rc;
-            points.resize(4 * std::max<uint64_t>(total, 1));
-            if ((rc = foort_gpu_positions(ctx, px.data(), n, res.data(), counts.data(), points.data(), total, &total)))
+            uint64_t total_pts = 0;
+            if ((rc = foort_gpu_positions(ctx, px.data(), n, res.data(), counts.data(), nullptr, 0, &total_pts)))
+                return rc;
+            points.resize(4 * std::max<uint64_t>(total_pts, 1));
+            if ((rc = foort_gpu_positions(ctx, px.data(), n, res.data(), counts.data(), points.data(), total_pts,
+                                          &total_pts)))
                 return rc;
             uint64_t s = 0;
             for (uint64_t g = 0; g < n; ++g) {
@@ -68,7 +186,7 @@ extern "C" int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_ou
                 s += counts[g];
             }
         }
-        k = 0;
+        uint64_t k = 0;
         for (uint32_t i = 0; i < n_images; ++i) {
             if (foort_mesh_is_finished(meshes[i])) continue;
             if (value_first == FOORT_DIAG_GEODESIC_POSITION) {
@@ -103,4 +221,17 @@ extern "C" int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_ou
     if (geodesics) *geodesics = total;
     if (rounds) *rounds = n_rounds;
     return FOORT_OK;
+}
+
+}  // namespace
+
+extern "C" int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs,
+                             uint32_t n_images, uint64_t* geodesics, uint32_t* rounds) {
+    if (!ctx || !meshes || n_images == 0) return FOORT_E_BADARG;
+    for (uint32_t i = 0; i < n_images; ++i)
+        if (!meshes[i]) return FOORT_E_BADARG;
+    uint32_t launches = 0, schedule = FOORT_SCHEDULE_ROUNDS;
+    const int rc = run(ctx, meshes, outputs, n_images, geodesics, rounds, launches, schedule);
+    foort_ctx_set_run_info(ctx, launches, schedule);
+    return rc;
 }

@@ -61,14 +61,19 @@ def sharded_round(px, integrate, rank, world, dist=None):
     return out
 
 
-def sharded_run(mesh_specs, desc, integrate, rank, world, dist=None, on_round=None):
+def sharded_run(mesh_specs, desc, integrate, rank, world, dist=None, on_round=None, waves=False):
     """One FOORT run (Main.cpp:313-419) sharded over `world` ranks. Every rank holds an
     identical copy of the meshes, so every rank computes the same pixel list for a round;
     each rank integrates its contiguous slice with integrate(slice) -> results, the slices
     are gathered (sharded_round), and every rank hands the whole round's results to its
     meshes (Mesh::GeodesicFinished, Main.cpp:399) before they end the round
     (Mesh::EndCurrentLoop, Main.cpp:410). The gather is the run's only exchange, once per
-    round. Returns the number of rounds; on_round(px, res) sees each whole round."""
-    from . import run_rounds
-    return run_rounds(mesh_specs, desc, lambda px: sharded_round(px, integrate, rank, world, dist), on_round)
+    round. waves: the meshes' level waves are sharded and gathered instead (one exchange
+    per wave) and the rounds replayed from their results (foort_gb300.run_by_waves).
+    Returns the number of rounds; on_round(px, res) sees each whole round."""
+    from . import run_by_waves, run_rounds
+    shard = lambda px: sharded_round(px, integrate, rank, world, dist)  # noqa: E731
+    if waves:
+        return run_by_waves(mesh_specs, desc, shard, on_round)[0]
+    return run_rounds(mesh_specs, desc, shard, on_round)
 

@@ -422,6 +422,16 @@ int foort_mesh_end_current_loop(foort_mesh* mesh);
 
 void foort_mesh_destroy(foort_mesh* mesh);
 
+/* The mesh's level waves: a new, unstarted mesh with the same parameters whose rounds
+ * subdivide every square of positive weight (IterationPixels unlimited), so that its
+ * round k hands out the pixels of subdivision level k. For a SquareSubdivisionMeshV2 with
+ * unlimited MaxPixels (0) the reference's rounds go on until no square of positive weight
+ * is left, so both meshes hand out the same pixels, the waves in max_subdivide rounds or
+ * fewer; a SimpleSquareMesh is its own single wave. FOORT_E_UNSUPPORTED for a V2 mesh
+ * with a finite MaxPixels (the cut depends on the round order) and for a mesh that has
+ * ended a round. Engine extension: the reference has no such schedule. */
+int foort_mesh_create_waves(const foort_mesh* mesh, foort_mesh** out);
+
 /* The mesh's Mesh::getFullDescriptionStr() (Mesh.cpp:69-73, 697-707) into buf. */
 int foort_mesh_description(const foort_mesh* mesh, char* buf, uint64_t cap);
 
@@ -560,6 +570,23 @@ int foort_timestamp_string(char* buf, uint64_t cap);
  * geodesics / rounds receive the totals. */
 int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs, uint32_t n_images,
                   uint64_t* geodesics, uint32_t* rounds);
+
+/* Schedule of foort_gpu_run's launches. Engine extension: the reference integrates
+ * round after round (Main.cpp:313-419).
+ *   FOORT_SCHEDULE_WAVES (default): where every mesh has level waves
+ *     (foort_mesh_create_waves), no step budget is set and GeodesicPosition is off, the
+ *     run integrates the waves -- one launch per subdivision level, over all images --
+ *     and then replays the meshes' rounds from the stored results. The meshes, the output
+ *     files and the returned counts see the reference's rounds in the reference's order,
+ *     and each result is the one the round's own launch would give (a geodesic's result
+ *     does not depend on the launch it runs in). A pixel of a round that no wave held is
+ *     integrated then, in one launch per such round. Elsewhere the run goes round by round.
+ *   FOORT_SCHEDULE_ROUNDS: one launch per round.
+ * foort_gpu_run_info reports the last run's launch count and the schedule it used. */
+#define FOORT_SCHEDULE_WAVES 0u
+#define FOORT_SCHEDULE_ROUNDS 1u
+int foort_gpu_set_schedule(foort_ctx* ctx, uint32_t schedule);
+int foort_gpu_run_info(const foort_ctx* ctx, uint32_t* launches, uint32_t* schedule);
 
 #ifdef __cplusplus
 }

@@ -17,9 +17,12 @@ from test_output import DAT, GEOPOS, RUNS, compare_dirs, geopos_workload
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("schedule", [abi.SCHEDULE_WAVES, abi.SCHEDULE_ROUNDS])
 @pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
 @pytest.mark.parametrize("name", sorted(RUNS))
-def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision):
+def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision, schedule):
+    """Both schedules of foort_gpu_run: the V2 run's level waves take three launches for
+    the reference's rounds, and the files are the reference's either way."""
     import foort_gb300
     foort_gb300.check_layout()
     wl = workloads.johannsen_golden(True, precision=precision)
@@ -29,10 +32,17 @@ def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision):
                              first_line=mesh.first_line_info(wl.desc), outputs_to_cache=run["cache"],
                              geodesics_per_file=run["per_file"])
     with foort_gb300.Engine(wl.desc) as e:
+        e.set_schedule(schedule)
         geodesics, rounds = e.run([mesh], [out])
+        launches, used = e.run_info()
     out.close()
     mesh.close()
-    print(f"{name}: {geodesics} geodesics in {rounds} rounds")
+    print(f"{name}: {geodesics} geodesics in {rounds} rounds, {launches} launches")
+    assert used == schedule
+    if schedule == abi.SCHEDULE_ROUNDS or name.startswith("simple"):
+        assert launches == rounds
+    else:
+        assert launches <= min(3, rounds)  # MaxSubdivide 3
     compare_dirs(tmp_path, name)
 
 

@@ -95,3 +95,61 @@ def test_v2_mesh_hands_out_the_reference_c2_run(engine_lib):
     mesh.close()
     assert k == len(rows) == 26547
     assert r == int(f["rounds"]) == 5
+
+
+def drive_values(mesh, value_of):
+    rounds = []
+    while not mesh.finished():
+        px = mesh.pixels()
+        rounds.append(px)
+        mesh.set_values(value_of(px["row"].astype(np.int64), px["col"].astype(np.int64)))
+        mesh.end_round()
+    return rounds
+
+
+def cells(rounds, grid):
+    allpx = np.concatenate(rounds)
+    return np.sort(allpx["row"].astype(np.int64) * grid + allpx["col"].astype(np.int64))
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c.startswith("v2")])
+def test_level_waves_hand_out_the_reference_pixel_set(engine_lib, case):
+    """foort_mesh_create_waves: with unlimited MaxPixels the waves hand out exactly the
+    pixels of the reference's rounds (each once), in at most MaxSubdivide waves; with a
+    finite MaxPixels there are no waves."""
+    import foort_gb300
+    kind, init, maxsub, iterpix, maxpix, stf, vd, vk = [int(v) for v in TRACES[case + "_spec"]]
+    mesh = foort_gb300.Mesh("v2", int(vd), int(vd), max_pixels=maxpix, initial_pixels=init, max_subdivide=maxsub,
+                            iteration_pixels=iterpix, initial_sub_to_final=stf)
+    grid = mesh.grid()
+    if maxpix:
+        with pytest.raises(foort_gb300.FoortError):
+            mesh.waves()
+        return
+    waves = mesh.waves()
+    assert waves.grid() == grid
+    got = drive_values(waves, lambda r, c: np.array([oracle.synth_value(vk, a, b, grid) for a, b in zip(r, c)]))
+    want = np.sort(TRACES[case + "_rows"].astype(np.int64) * grid + TRACES[case + "_cols"].astype(np.int64))
+    assert np.array_equal(cells(got, grid), want)
+    assert len(got) <= maxsub
+    # a mesh that has ended a round has no waves
+    mesh.set_values([0.0] * mesh.size())
+    mesh.end_round()
+    with pytest.raises(foort_gb300.FoortError):
+        mesh.waves()
+
+
+def test_level_waves_of_the_reference_c2_run(engine_lib):
+    """The C2 mesh's waves given the reference run's quadrants: the run's 26,547 pixels in
+    three waves (the reference takes five rounds)."""
+    import foort_gb300
+    from foort_gb300 import workloads
+    f = c2_run_fixture()
+    rows, cols = f["row"].astype(np.int64), f["col"].astype(np.int64)
+    wl = workloads.c2()
+    mesh = foort_gb300.Mesh.from_spec(wl.mesh[0], wl.desc.diag_flags, wl.desc.value_diag)
+    quad = np.full((509, 509), -1.0)
+    quad[rows, cols] = f["quadrant"]
+    got = drive_values(mesh.waves(), lambda r, c: quad[r, c])
+    assert [len(w) for w in got] == [16384, 3125, 7038]
+    assert np.array_equal(cells(got, 509), np.sort(rows * 509 + cols))

@@ -76,7 +76,7 @@ def _c2_shaped():
     return d, mesh, keep
 
 
-def _run_main(rank, world, port, outdir):
+def _run_main(rank, world, port, outdir, waves=False):
     import torch.distributed as dist
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
     dist.init_process_group("gloo", rank=rank, world_size=world)
@@ -90,7 +90,7 @@ def _run_main(rank, world, port, outdir):
             return oracle.integrate(d, p, fast=False, nthreads=1)
 
         rounds = multirank.sharded_run(mesh, d, integrate, rank, world, dist,
-                                       on_round=lambda px, res: seen.append((px.copy(), res.copy())))
+                                       on_round=lambda px, res: seen.append((px.copy(), res.copy())), waves=waves)
         np.savez(os.path.join(outdir, f"run{rank}.npz"), px=np.concatenate([p for p, _ in seen]),
                  res=np.concatenate([r for _, r in seen]), sizes=np.array([len(p) for p, _ in seen]),
                  mine=np.array(mine), rounds=rounds)
@@ -99,15 +99,18 @@ def _run_main(rank, world, port, outdir):
         dist.destroy_process_group()
 
 
-def test_sharded_c2_shaped_run_hands_out_the_single_rank_pixels(oracle_mod, tmp_path):
+@pytest.mark.parametrize("waves", [False, True])
+def test_sharded_c2_shaped_run_hands_out_the_single_rank_pixels(oracle_mod, tmp_path, waves):
     """A whole adaptive run (Main.cpp:313-419) over two gloo ranks, each integrating its
     contiguous half of every round with the oracle and gathering before the mesh ends the
     round (Mesh.cpp:1092-1186), must hand out the same pixels in the same order, with the
-    same results, as the run on one rank; each rank integrated only its half."""
+    same results, as the run on one rank; each rank integrated only its half. With waves
+    the ranks split the level waves instead and replay the same rounds."""
     import foort_gb300
     import torch.multiprocessing as mp
     world = 2
-    mp.start_processes(_run_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    mp.start_processes(_run_main, args=(world, _free_port(), str(tmp_path), waves), nprocs=world,
+                       start_method="spawn")
     d, mesh, keep = _c2_shaped()
     seen = []
     rounds = foort_gb300.run_rounds(mesh, d, lambda p: oracle_mod.integrate(d, p, fast=False),
@@ -123,6 +126,14 @@ def test_sharded_c2_shaped_run_hands_out_the_single_rank_pixels(oracle_mod, tmp_
             np.testing.assert_array_equal(f["px"][name], want_px[name], err_msg=name)
         for name in abi.RESULT_DTYPE.names:
             np.testing.assert_array_equal(f["res"][name], want_res[name], err_msg=name)
-        halves = [multirank.shard_range(n, r, world) for n in sizes]
+        if waves:
+            d2, mesh2, keep2 = _c2_shaped()
+            wsizes = []
+            foort_gb300.run_rounds(mesh2, d2, lambda p: oracle_mod.integrate(d2, p, fast=False),
+                                   on_round=lambda px, res: wsizes.append(len(px)), waves=True)
+            assert len(wsizes) < len(sizes) and sum(wsizes) == sum(sizes)
+            halves = [multirank.shard_range(n, r, world) for n in wsizes]
+        else:
+            halves = [multirank.shard_range(n, r, world) for n in sizes]
         assert list(f["mine"]) == [hi - lo for lo, hi in halves]
     del keep
