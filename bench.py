@@ -13,10 +13,12 @@ One step = one whole run of the workload (every geodesic of its mesh once):
          launch each through foort_gpu_integrate_async on one stream; CUDA events on that
          stream around each step; L2 flushed (256 MB write) between steps; the launch
          shape of each launch chosen by the engine's autotuner (foort_gpu_autotune) in
-         the first warm-up step. The launches are the schedule's (--schedule): the
-         meshes' level waves, one launch per subdivision level (foort_gpu_run's default;
-         C2: 3 launches for the reference's 5 rounds, the same 26,547 pixels), or one per
-         round;
+         the first warm-up step. The launches are the schedule's (--schedule): those
+         foort_gpu_run makes by default, the meshes' level waves with lookahead (one
+         launch per subdivision level, a launch also taking the next level's candidates
+         while it stays small enough; C2: 2 launches of 16,384 and 14,367 geodesics for
+         the reference's 5 rounds of 26,547), or one per round. value counts the run's
+         geodesics only;
   e2e    the whole run through the public C ABI, foort_gpu_run: host meshes, H2D of each
          launch's pixels, kernel, D2H of its results, and the meshes' rounds replayed in
          the reference's order. e2e_per_round_api: the same run through the per-round
@@ -342,6 +344,19 @@ def run_profile_case(args):
     return 0
 
 
+def pixel_index(have, want):
+    """Index into `have` of each pixel of `want` (both PIXEL_DTYPE arrays; every pixel of
+    `want` must be in `have`)."""
+    def key(p):
+        return (p["image"].astype(np.int64) << 42) | (p["row"].astype(np.int64) * p["grid"].astype(np.int64)
+                                                     + p["col"].astype(np.int64))
+    kh, kw = key(have), key(want)
+    order = np.argsort(kh, kind="stable")
+    i = order[np.searchsorted(kh[order], kw)]
+    assert np.array_equal(kh[i], kw)
+    return i
+
+
 def config_block(wl, args, side=None, rounds=None, geod=None):
     c = {"workload": wl.name, "model": None, "global_batch": geod, "rounds": rounds,
          "metric_params": list(wl.images[0].metric_params)[:2], "iteration_pixels": None,
@@ -449,11 +464,20 @@ def main():
     mkind = kind_of(wl)
     t0 = time.perf_counter()
     rounds = adaptive_rounds(foort_gb300, wl)
-    launches_px = adaptive_rounds(foort_gb300, wl, waves=True) if args.schedule == "waves" else rounds
+    launches_px = rounds
+    if args.schedule == "waves":  # the launches foort_gpu_run makes (waves with lookahead)
+        with foort_gb300.Engine(wl.desc) as e:
+            e.set_record_launches(True)
+            meshes = [foort_gb300.Mesh.from_spec(spec, wl.desc.diag_flags, wl.desc.value_diag) for spec in wl.mesh]
+            e.run(meshes)
+            for m in meshes:
+                m.close()
+            launches_px = e.run_launches()
     log(f"[bench] {wl.name}: {len(rounds)} rounds, sizes {[len(r) for r in rounds]}; {args.schedule}: "
         f"{[len(r) for r in launches_px]}; prepare {time.perf_counter() - t0:.1f}s")
     n_geod = sum(len(r) for r in rounds)
-    assert sum(len(r) for r in launches_px) == n_geod
+    n_launched = sum(len(r) for r in launches_px)
+    assert n_launched >= n_geod
     stream = torch.cuda.Stream()
 
     def to_device(lists):
@@ -575,11 +599,11 @@ def main():
         barrier()
         t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps)
     n_launch_run, sched_used = run_launches[-1]
-    # every pixel goes up once and its result comes back once when the launches are the
-    # schedule's (no pixel integrated twice)
+    # each launched pixel goes up once and its result comes back once: the launches are
+    # the recorded ones
     assert n_launch_run == len(launches_px), (n_launch_run, len(launches_px))
-    e2e = {"value": world * n_geod / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n_geod * abi.PIXEL_DTYPE.itemsize,
-           "d2h_bytes_per_step": n_geod * abi.RESULT_DTYPE.itemsize, "ms_per_step": t_e2e * 1e3,
+    e2e = {"value": world * n_geod / t_e2e, "unit": UNIT, "h2d_bytes_per_step": n_launched * abi.PIXEL_DTYPE.itemsize,
+           "d2h_bytes_per_step": n_launched * abi.RESULT_DTYPE.itemsize, "ms_per_step": t_e2e * 1e3,
            "api": "foort_gpu_run", "launches_per_step": n_launch_run,
            "schedule": "level waves" if sched_used == abi.SCHEDULE_WAVES else "rounds"}
 
@@ -677,8 +701,10 @@ def main():
                 "roofline_fp64": {"achieved": steps64 * OPS_PER_STEP.get(mkind, 1130) / (t64 * 1e-3) / 1e12,
                                   "peak": peaks[1], "unit": "TFLOP/s",
                                   "frac": steps64 * OPS_PER_STEP.get(mkind, 1130) / (t64 * 1e-3) / 1e12 / peaks[1]}}
-        acc = accuracy_legs(foort_gb300, args, wl, np.concatenate(launches_px), np.concatenate(mixed_res),
-                            np.concatenate(res64))
+        run_px = np.concatenate(rounds)  # the run's own pixels (no looked-ahead ones)
+        pick = pixel_index(np.concatenate(launches_px), run_px)
+        acc = accuracy_legs(foort_gb300, args, wl, run_px, np.concatenate(mixed_res)[pick],
+                            np.concatenate(res64)[pick])
 
     # ---- roofline of the dominant kernel: the mixed kernel over all launches of a step
     # (each round is one launch of it), and its largest launch alone
@@ -744,8 +770,11 @@ def main():
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "mixed-f32 (FP32 right-hand side; float-float state and decisions)", "data": "synthetic",
         "config": dict(config_block(wl, args, rounds=len(rounds), geod=n_geod),
-                       schedule=("level waves: one launch per subdivision level, the reference's rounds replayed "
-                                 "from their results" if launches_px is not rounds else "one launch per round"),
+                       schedule=("level waves with lookahead (foort_gpu_run's launches): one launch per "
+                                 "subdivision level, a launch also taking the next level's candidates while it "
+                                 "holds at most 128 x SMs geodesics; the reference's rounds replayed from the "
+                                 "results; value counts the run's geodesics only"
+                                 if launches_px is not rounds else "one launch per round"),
                        autotuned=not args.no_tune, launch_shapes=tuned_shapes),
         "geodesics_per_step": world * n_geod, "steps_per_s": world * steps_total / (t_step * 1e-3),
         "gpu_launches": args.steps * len(launches_px),
@@ -755,6 +784,7 @@ def main():
         "accuracy": acc,
         "round_sizes": [len(r) for r in rounds],
         "launch_sizes": [len(r) for r in launches_px],
+        "geodesics_launched_per_step": world * n_launched,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

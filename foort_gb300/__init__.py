@@ -105,6 +105,10 @@ def load():
     lib.foort_tune_save.argtypes = [C.c_char_p]
     lib.foort_tune_load.argtypes = [C.c_char_p]
     lib.foort_mesh_create_waves.argtypes = [vp, C.POINTER(vp)]
+    lib.foort_mesh_lookahead.argtypes = [vp, u32, vp, u64, C.POINTER(u64)]
+    lib.foort_gpu_set_lookahead.argtypes = [vp, u64]
+    lib.foort_gpu_set_record_launches.argtypes = [vp, i32]
+    lib.foort_gpu_run_launch.argtypes = [vp, u32, vp, u64, C.POINTER(u64)]
     lib.foort_gpu_set_schedule.argtypes = [vp, u32]
     lib.foort_gpu_run_info.argtypes = [vp, C.POINTER(u32), C.POINTER(u32)]
     lib.foort_dmesh_create_v2.argtypes = [u64, u64, i32, u64, i32, u32, u32, u32, u32, vp, C.POINTER(vp)]
@@ -251,6 +255,27 @@ class Engine:
         """foort_gpu_run's launches: level waves where they apply, or one per round."""
         self._check(self._lib.foort_gpu_set_schedule(self._ctx, schedule))
 
+    def set_lookahead(self, max_geodesics=None):
+        """Cap of a wave launch that also takes the next wave's candidates (None: the
+        default, 128 x the SM count; 0: off)."""
+        self._check(self._lib.foort_gpu_set_lookahead(self._ctx, (1 << 64) - 1 if max_geodesics is None
+                                                      else max_geodesics))
+
+    def set_record_launches(self, on=True):
+        self._check(self._lib.foort_gpu_set_record_launches(self._ctx, 1 if on else 0))
+
+    def run_launches(self):
+        """The pixel lists of the last run's launches (set_record_launches)."""
+        out, k = [], 0
+        n = C.c_uint64()
+        while self._lib.foort_gpu_run_launch(self._ctx, k, None, 0, C.byref(n)) == 0:
+            a = np.zeros(n.value, dtype=abi.PIXEL_DTYPE)
+            if n.value:
+                self._check(self._lib.foort_gpu_run_launch(self._ctx, k, a.ctypes.data, n.value, C.byref(n)))
+            out.append(a)
+            k += 1
+        return out
+
     def run_info(self):
         """(launches, schedule) of the last foort_gpu_run."""
         n, sch = C.c_uint32(), C.c_uint32()
@@ -385,6 +410,17 @@ class Mesh:
 
     def end_round(self):
         self._lib.foort_mesh_end_current_loop(self._m)
+
+    def lookahead(self, image=0):
+        """foort_mesh_lookahead: candidates of the next round of a mesh of level waves."""
+        n = C.c_uint64()
+        rc = self._lib.foort_mesh_lookahead(self._m, image, None, 0, C.byref(n))
+        if rc != 0:
+            raise FoortError(rc, "lookahead failed")
+        out = np.zeros(n.value, dtype=abi.PIXEL_DTYPE)
+        if n.value:
+            self._lib.foort_mesh_lookahead(self._m, image, out.ctypes.data, n.value, C.byref(n))
+        return out
 
     def waves(self):
         """The mesh's level waves (foort_mesh_create_waves) as a new Mesh."""

@@ -42,7 +42,10 @@ struct foort_ctx {
     bool pending = false;
     bool autotune = false;  // search shapes for launches without a cache entry
     uint32_t schedule = FOORT_SCHEDULE_WAVES;  // foort_gpu_run
+    uint64_t lookahead = FOORT_LOOKAHEAD_AUTO;
     uint32_t run_launches = 0, run_schedule = 0;
+    bool record = false;  // keep the last run's launch pixel lists
+    std::vector<std::vector<foort_pixel>> launch_px;
     foort_stats stats{};
     std::string err;
 };
@@ -708,7 +711,37 @@ int foort_gpu_run_info(const foort_ctx* ctx, uint32_t* launches, uint32_t* sched
     return FOORT_OK;
 }
 
+int foort_gpu_set_lookahead(foort_ctx* ctx, uint64_t max_geodesics) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    ctx->lookahead = max_geodesics;
+    return FOORT_OK;
+}
+
+int foort_gpu_set_record_launches(foort_ctx* ctx, int32_t on) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    ctx->record = on != 0;
+    if (!ctx->record) ctx->launch_px.clear();
+    return FOORT_OK;
+}
+
+int foort_gpu_run_launch(const foort_ctx* ctx, uint32_t k, foort_pixel* out, uint64_t cap, uint64_t* n) {
+    if (!ctx || !n || k >= ctx->launch_px.size()) return FOORT_E_BADARG;
+    const auto& v = ctx->launch_px[k];
+    *n = v.size();
+    if (!out) return FOORT_OK;
+    if (cap < v.size()) return FOORT_E_BADARG;
+    std::copy(v.begin(), v.end(), out);
+    return FOORT_OK;
+}
+
 uint32_t foort_ctx_schedule(const foort_ctx* ctx) { return ctx->schedule; }
+uint64_t foort_ctx_lookahead(const foort_ctx* ctx) {
+    return ctx->lookahead == FOORT_LOOKAHEAD_AUTO ? 128ull * static_cast<uint64_t>(ctx->num_sms) : ctx->lookahead;
+}
+void foort_ctx_launched(foort_ctx* ctx, const foort_pixel* px, uint64_t n, bool first) {
+    if (first) ctx->launch_px.clear();
+    if (ctx->record) ctx->launch_px.emplace_back(px, px + n);
+}
 uint64_t foort_ctx_budget(const foort_ctx* ctx) { return ctx->budget; }
 void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule) {
     ctx->run_launches = launches;

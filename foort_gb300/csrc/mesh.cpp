@@ -67,6 +67,9 @@ struct foort_mesh {
     // The same mesh, unstarted, with every square of positive weight subdivided in each
     // round (foort_mesh_create_waves); null where that is not this mesh's pixel set.
     virtual foort_mesh* wave_clone() const = 0;
+    // Every pixel the next round could hand out: the five candidates of each square that
+    // awaits its weight (foort_mesh_lookahead); cells, each once.
+    virtual void lookahead(std::vector<uint64_t>&) const {}
 };
 
 namespace {
@@ -263,6 +266,22 @@ struct V2Mesh final : foort_mesh {
         return m;
     }
 
+    // The squares of the updating list get their weights at the end of this round; the
+    // next round subdivides some of them (all that get a positive weight, in a wave mesh),
+    // and each subdivision hands out at most its square's p2, p4, p5, p6 and p8.
+    void lookahead(std::vector<uint64_t>& cells) const override {
+        cells.clear();
+        cells.reserve(5 * updating.size());
+        for (const Px* p : updating) {
+            const uint64_t h = pow2(max_sub - p->level - 1);  // half the square's side
+            const uint64_t r = p->row, c = p->col;
+            const uint64_t cand[5][2] = {{r, c + h}, {r + h, c}, {r + h, c + h}, {r + h, c + 2 * h}, {r + 2 * h, c + h}};
+            for (const auto& q : cand) cells.push_back(q[0] * grid + q[1]);
+        }
+        std::sort(cells.begin(), cells.end());
+        cells.erase(std::unique(cells.begin(), cells.end()), cells.end());
+    }
+
     // EndCurrentLoop, Mesh.cpp:1092-1186
     void end_loop() override {
         ++n_rounds;
@@ -374,6 +393,18 @@ int foort_mesh_end_current_loop(foort_mesh* m) {
 }
 
 void foort_mesh_destroy(foort_mesh* m) { delete m; }
+
+int foort_mesh_lookahead(const foort_mesh* m, uint32_t image, foort_pixel* out, uint64_t cap, uint64_t* n) {
+    if (!m || !n) return FOORT_E_BADARG;
+    std::vector<uint64_t> cells;
+    m->lookahead(cells);
+    *n = cells.size();
+    if (!out) return FOORT_OK;
+    if (cap < cells.size()) return FOORT_E_BADARG;
+    for (uint64_t i = 0; i < cells.size(); ++i)
+        out[i] = foort_pixel{image, 0u, cells[i] / m->grid, cells[i] % m->grid, m->grid};
+    return FOORT_OK;
+}
 
 int foort_mesh_create_waves(const foort_mesh* m, foort_mesh** out) {
     if (!m || !out) return FOORT_E_BADARG;

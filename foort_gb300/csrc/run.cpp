@@ -28,7 +28,9 @@
 extern "C" {
 uint32_t foort_ctx_schedule(const foort_ctx* ctx);
 uint64_t foort_ctx_budget(const foort_ctx* ctx);
+uint64_t foort_ctx_lookahead(const foort_ctx* ctx);
 void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule);
+void foort_ctx_launched(foort_ctx* ctx, const foort_pixel* px, uint64_t n, bool first);
 }
 
 namespace {
@@ -65,6 +67,36 @@ struct ResultStore {
 
 uint64_t cell_of(const foort_pixel& p) { return p.row * p.grid + p.col; }
 
+// One launch of the run (foort_gpu_integrate), counted and recorded.
+int launch(foort_ctx* ctx, const std::vector<foort_pixel>& px, std::vector<foort_result>& res, uint32_t& launches) {
+    res.resize(px.size());
+    foort_ctx_launched(ctx, px.data(), px.size(), launches == 0);
+    ++launches;
+    return foort_gpu_integrate(ctx, px.data(), px.size(), res.data());
+}
+
+// The next wave's candidates (foort_mesh_lookahead) that have no result yet and are not
+// in `todo`, appended to `spec`.
+int lookahead_candidates(foort_mesh* const* waves, uint32_t n_images, const ResultStore& store,
+                         const std::vector<foort_pixel>& todo, std::vector<foort_pixel>& spec) {
+    std::vector<std::unordered_map<uint64_t, uint64_t>> now(n_images);
+    for (const foort_pixel& p : todo) now[p.image].emplace(cell_of(p), 0);
+    std::vector<foort_pixel> cand;
+    for (uint32_t i = 0; i < n_images; ++i) {
+        if (foort_mesh_is_finished(waves[i])) continue;
+        uint64_t n = 0;
+        int rc = foort_mesh_lookahead(waves[i], i, nullptr, 0, &n);
+        if (rc) return rc;
+        cand.resize(n);
+        if (n && (rc = foort_mesh_lookahead(waves[i], i, cand.data(), n, &n))) return rc;
+        for (const foort_pixel& p : cand) {
+            const uint64_t c = cell_of(p);
+            if (!store.slot[i].count(c) && !now[i].count(c)) spec.push_back(p);
+        }
+    }
+    return FOORT_OK;
+}
+
 // Integrate the meshes' level waves, one launch per wave over all images, and keep every
 // result. FOORT_E_UNSUPPORTED (nothing integrated) where a mesh has no waves.
 int integrate_waves(foort_ctx* ctx, foort_mesh* const* meshes, uint32_t n_images, ResultStore& store,
@@ -80,23 +112,35 @@ int integrate_waves(foort_ctx* ctx, foort_mesh* const* meshes, uint32_t n_images
         }
     }
     store.slot.assign(n_images, {});
-    std::vector<foort_pixel> px;
-    std::vector<foort_result> res;
+    const uint64_t ahead = foort_ctx_lookahead(ctx);
+    std::vector<foort_pixel> px, todo;
+    std::vector<foort_result> res, got;
     std::vector<uint64_t> count(n_images);
     int rc = FOORT_OK;
     for (;;) {
         bool any = false;
         if ((rc = gather(waves.data(), n_images, px, count, any)) || !any) break;
+        // this wave's pixels without a result (none where the last launch looked ahead)
+        todo.clear();
+        for (const foort_pixel& p : px)
+            if (!store.slot[p.image].count(cell_of(p))) todo.push_back(p);
+        if (!todo.empty()) {
+            if (ahead > todo.size()) {
+                std::vector<foort_pixel> spec;
+                if ((rc = lookahead_candidates(waves.data(), n_images, store, todo, spec))) break;
+                if (todo.size() + spec.size() <= ahead) todo.insert(todo.end(), spec.begin(), spec.end());
+            }
+            if ((rc = launch(ctx, todo, got, launches))) break;
+            for (uint64_t g = 0; g < todo.size(); ++g) {
+                store.slot[todo[g].image][cell_of(todo[g])] = store.res.size();
+                store.res.push_back(got[g]);
+            }
+        }
         res.resize(px.size());
-        if ((rc = foort_gpu_integrate(ctx, px.data(), px.size(), res.data()))) break;
-        ++launches;
+        for (uint64_t g = 0; g < px.size(); ++g) res[g] = store.res[store.slot[px[g].image].at(cell_of(px[g]))];
         uint64_t k = 0;
         for (uint32_t i = 0; i < n_images && rc == FOORT_OK; ++i) {
             if (foort_mesh_is_finished(waves[i])) continue;
-            for (uint64_t g = k; g < k + count[i]; ++g) {
-                store.slot[i][cell_of(px[g])] = store.res.size();
-                store.res.push_back(res[g]);
-            }
             rc = foort_mesh_set_results(waves[i], res.data() + k, count[i]);
             if (!rc) rc = foort_mesh_end_current_loop(waves[i]);
             k += count[i];
@@ -122,10 +166,9 @@ int results_from_store(foort_ctx* ctx, const ResultStore& store, const std::vect
     }
     if (miss.empty()) return FOORT_OK;
     std::vector<foort_pixel> mp(miss.size());
-    std::vector<foort_result> mr(miss.size());
+    std::vector<foort_result> mr;
     for (uint64_t j = 0; j < miss.size(); ++j) mp[j] = px[miss[j]];
-    const int rc = foort_gpu_integrate(ctx, mp.data(), mp.size(), mr.data());
-    ++launches;
+    const int rc = launch(ctx, mp, mr, launches);
     if (rc) return rc;
     for (uint64_t j = 0; j < miss.size(); ++j) res[miss[j]] = mr[j];
     return FOORT_OK;
@@ -163,8 +206,7 @@ int run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs,
         if (schedule == FOORT_SCHEDULE_WAVES) {
             rc = results_from_store(ctx, store, px, res, launches);
         } else {
-            rc = foort_gpu_integrate(ctx, px.data(), n, res.data());
-            ++launches;
+            rc = launch(ctx, px, res, launches);
         }
         if (rc != FOORT_OK) return rc;
         // GeodesicPosition: a second pass records the positions (foort_gpu_positions)

@@ -432,6 +432,14 @@ void foort_mesh_destroy(foort_mesh* mesh);
  * ended a round. Engine extension: the reference has no such schedule. */
 int foort_mesh_create_waves(const foort_mesh* mesh, foort_mesh** out);
 
+/* The pixels that the squares whose weight the end of this round decides can add: the top
+ * and left edge midpoints, the centre and the right and bottom edge midpoints of each, as
+ * pixels of `image` in row-major order (V2 meshes; none for a SimpleSquareMesh). In a mesh
+ * of level waves (foort_mesh_create_waves), where every square of positive weight is
+ * subdivided in the next round, the next round hands out a subset of them. *n receives the
+ * count; with out == NULL only the count, otherwise cap must hold it. Engine extension. */
+int foort_mesh_lookahead(const foort_mesh* mesh, uint32_t image, foort_pixel* out, uint64_t cap, uint64_t* n);
+
 /* The mesh's Mesh::getFullDescriptionStr() (Mesh.cpp:69-73, 697-707) into buf. */
 int foort_mesh_description(const foort_mesh* mesh, char* buf, uint64_t cap);
 
@@ -587,6 +595,23 @@ int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const
 #define FOORT_SCHEDULE_ROUNDS 1u
 int foort_gpu_set_schedule(foort_ctx* ctx, uint32_t schedule);
 int foort_gpu_run_info(const foort_ctx* ctx, uint32_t* launches, uint32_t* schedule);
+
+/* Lookahead of the wave schedule. A launch lasts about as long as its slowest geodesic
+ * while the GPU has idle lanes, so the launch of a wave may also take the next wave's
+ * candidates (foort_mesh_lookahead: a superset of the next wave) as long as the launch
+ * then holds at most max_geodesics geodesics; the next wave then needs no launch of its
+ * own. Candidates the run does not use are integrated and dropped: they reach neither
+ * the meshes nor the files. 0 = off; FOORT_LOOKAHEAD_AUTO (default) = 128 x the GPU's SM
+ * count (19,456 on GB300), about the geodesics a launch holds at two lanes each before
+ * its warps share issue slots. */
+#define FOORT_LOOKAHEAD_AUTO UINT64_MAX
+int foort_gpu_set_lookahead(foort_ctx* ctx, uint64_t max_geodesics);
+
+/* on = 1: foort_gpu_run keeps the pixel list of each launch of the run (the last run's
+ * only); foort_gpu_run_launch copies launch k's list to out (count in *n; out == NULL:
+ * count only). For benchmarks that replay a run's launches from device memory. */
+int foort_gpu_set_record_launches(foort_ctx* ctx, int32_t on);
+int foort_gpu_run_launch(const foort_ctx* ctx, uint32_t k, foort_pixel* out, uint64_t cap, uint64_t* n);
 
 #ifdef __cplusplus
 }

@@ -17,12 +17,14 @@ from test_output import DAT, GEOPOS, RUNS, compare_dirs, geopos_workload
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("schedule", [abi.SCHEDULE_WAVES, abi.SCHEDULE_ROUNDS])
+@pytest.mark.parametrize("schedule,lookahead", [(abi.SCHEDULE_WAVES, None), (abi.SCHEDULE_WAVES, 0),
+                                                (abi.SCHEDULE_ROUNDS, None)])
 @pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
 @pytest.mark.parametrize("name", sorted(RUNS))
-def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision, schedule):
-    """Both schedules of foort_gpu_run: the V2 run's level waves take three launches for
-    the reference's rounds, and the files are the reference's either way."""
+def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision, schedule, lookahead):
+    """Every schedule of foort_gpu_run: the V2 run's level waves take at most three
+    launches for the reference's rounds (fewer with lookahead), and the files are the
+    reference's either way."""
     import foort_gb300
     foort_gb300.check_layout()
     wl = workloads.johannsen_golden(True, precision=precision)
@@ -33,16 +35,23 @@ def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision, s
                              geodesics_per_file=run["per_file"])
     with foort_gb300.Engine(wl.desc) as e:
         e.set_schedule(schedule)
+        e.set_lookahead(lookahead)
+        e.set_record_launches(True)
         geodesics, rounds = e.run([mesh], [out])
         launches, used = e.run_info()
+        launched = e.run_launches()
     out.close()
     mesh.close()
     print(f"{name}: {geodesics} geodesics in {rounds} rounds, {launches} launches")
-    assert used == schedule
+    assert used == schedule and len(launched) == launches
     if schedule == abi.SCHEDULE_ROUNDS or name.startswith("simple"):
         assert launches == rounds
+        assert sum(len(p) for p in launched) == geodesics
     else:
         assert launches <= min(3, rounds)  # MaxSubdivide 3
+        assert sum(len(p) for p in launched) >= geodesics
+        if lookahead == 0:
+            assert sum(len(p) for p in launched) == geodesics
     compare_dirs(tmp_path, name)
 
 

@@ -153,3 +153,31 @@ def test_level_waves_of_the_reference_c2_run(engine_lib):
     got = drive_values(mesh.waves(), lambda r, c: quad[r, c])
     assert [len(w) for w in got] == [16384, 3125, 7038]
     assert np.array_equal(cells(got, 509), np.sort(rows * 509 + cols))
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c.startswith("v2")])
+def test_lookahead_holds_the_next_wave(engine_lib, case):
+    """foort_mesh_lookahead on a mesh of level waves: each round's candidates hold every
+    pixel of the next round, and none of them has been handed out before."""
+    import foort_gb300
+    kind, init, maxsub, iterpix, maxpix, stf, vd, vk = [int(v) for v in TRACES[case + "_spec"]]
+    if maxpix:
+        pytest.skip("no level waves with a finite MaxPixels")
+    mesh = foort_gb300.Mesh("v2", int(vd), int(vd), initial_pixels=init, max_subdivide=maxsub,
+                            iteration_pixels=iterpix, initial_sub_to_final=stf)
+    grid = mesh.grid()
+    waves = mesh.waves()
+    seen = set()
+    cand = None
+    while not waves.finished():
+        px = waves.pixels()
+        got = set((px["row"].astype(np.int64) * grid + px["col"].astype(np.int64)).tolist())
+        if cand is not None:
+            assert got <= cand
+        assert not (got & seen)
+        seen |= got
+        la = waves.lookahead()
+        cand = set((la["row"].astype(np.int64) * grid + la["col"].astype(np.int64)).tolist())
+        assert len(cand) == len(la) and np.all(la["grid"] == grid)
+        waves.set_values([oracle.synth_value(vk, a, b, grid) for a, b in zip(px["row"], px["col"])])
+        waves.end_round()
