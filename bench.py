@@ -662,10 +662,12 @@ def main():
 
         with foort_gb300.Engine(wl.desc) as e:
             e.set_lanes(args.lanes)
+            e.set_schedule(abi.SCHEDULE_WAVES if args.schedule == "waves" else abi.SCHEDULE_ROUNDS)
             dm = new_mesh()
             g_dm, r_dm = dm.run(e, d_res.data_ptr(), cap, lambda d_px, d_r, n, k: same.append(
                 k < len(rounds) and np.array_equal(dm.pixels(), rounds[k])))
             dm.close()
+            dm_launches, _ = e.run_info()
             barrier()
             t0 = time.perf_counter()
             for _ in range(args.steps):
@@ -675,8 +677,10 @@ def main():
             barrier()
             t_dm = max_over_ranks((time.perf_counter() - t0) / args.steps)
         dmesh = {"value": world * n_geod / t_dm, "unit": UNIT, "ms_per_step": t_dm * 1e3, "geodesics": g_dm,
-                 "rounds": r_dm, "same_pixels_as_host_mesh": len(same) == len(rounds) and all(same),
-                 "scope": "whole run, device-resident V2 mesh (reference order), results left in device memory"}
+                 "rounds": r_dm, "launches_per_step": dm_launches,
+                 "same_pixels_as_host_mesh": len(same) == len(rounds) and all(same),
+                 "scope": "whole run, device-resident V2 mesh (reference order) and the same schedule on the "
+                          "device, results left in device memory"}
 
     # ---- FP64 plain kernel on the same pixels (N = 1 only: under torchrun the other GPUs
     # would wait for it)

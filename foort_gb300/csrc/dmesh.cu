@@ -45,6 +45,7 @@
 #include <cuda_runtime.h>
 
 #include <cub/device/device_merge_sort.cuh>
+#include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_select.cuh>
 
 #include <algorithm>
@@ -219,6 +220,47 @@ __global__ void k_seed(uint64_t n, uint64_t scale, uint64_t R, int max_sub, int3
     }
 }
 
+// ---- level waves on the device (foort_gpu_run_dmesh with FOORT_SCHEDULE_WAVES)
+constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
+
+// Cells of q without a stored result.
+__global__ void k_flag_unstored(const uint64_t* q, uint64_t n, const uint32_t* slot, uint8_t* flag) {
+    DM_FOR(i, n) flag[i] = slot[q[i]] == kNoSlot ? 1 : 0;
+}
+
+// The five candidates of each updating pixel's square (p2, p4, p5, p6, p8 of a square of
+// half-side h = 2^(MaxSubdivide - level - 1)), flagged where no result is stored.
+__global__ void k_candidates(const uint64_t* upd, uint64_t nu, const int32_t* level, const uint32_t* slot, uint64_t R,
+                             int max_sub, uint64_t* out, uint8_t* flag) {
+    DM_FOR(i, nu) {
+        const uint64_t c = upd[i];
+        const uint64_t h = 1ull << (max_sub - level[c] - 1);
+        const uint64_t cand[5] = {c + h, c + h * R, c + h * R + h, c + h * R + 2 * h, c + 2 * h * R + h};
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            out[5 * i + j] = cand[j];
+            flag[5 * i + j] = slot[cand[j]] == kNoSlot ? 1 : 0;
+        }
+    }
+}
+
+// The launch's results are pool[base .. base + n): point the cells' slots at them.
+__global__ void k_set_slots(const uint64_t* cells, uint64_t n, uint32_t base, uint32_t* slot) {
+    DM_FOR(i, n) slot[cells[i]] = base + static_cast<uint32_t>(i);
+}
+
+// Values of the queued cells from their stored results.
+__global__ void k_values_from_pool(const uint64_t* q, uint64_t n, const uint32_t* slot, const foort_result* pool,
+                                   uint32_t kind, double* value) {
+    DM_FOR(i, n) value[q[i]] = result_value(kind, pool[slot[q[i]]]);
+}
+
+// The round's results in the round's order.
+__global__ void k_gather(const uint64_t* q, uint64_t n, const uint32_t* slot, const foort_result* pool,
+                         foort_result* out) {
+    DM_FOR(i, n) out[i] = pool[slot[q[i]]];
+}
+
 unsigned grid_for(uint64_t n) {
     return static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 152ull * 16)));
 }
@@ -228,7 +270,7 @@ uint64_t pow2(int e) { return 1ull << e; }
 }  // namespace
 
 struct foort_dmesh {
-    uint64_t R = 0, initial = 0, iteration = 0, max_pixels = 0, left_px = 0;
+    uint64_t R = 0, initial = 0, initial_arg = 0, iteration = 0, max_pixels = 0, left_px = 0;
     int max_sub = 1;
     bool infinite = true;
     uint32_t value_diag = 0, value_kind = 0, image = 0, order = 0;
@@ -257,10 +299,11 @@ struct foort_dmesh {
     ActiveSq* active = nullptr;  // FOORT_DMESH_ORDER_DEVICE
     ActiveSq* active_tmp = nullptr;
     uint64_t cap_a = 0;
-    long long* num = nullptr;  // device counters: 0 new actives, 1 queue, 2 updating
+    long long* num = nullptr;  // device counters: 0 new actives, 1 queue, 2 updating, 3 scratch
     void* tmp = nullptr;
     size_t tmp_bytes = 0;
     std::vector<ActiveSq> mirror;  // FOORT_DMESH_ORDER_REFERENCE: the active list
+    bool unordered = false;        // wave copy: the queue's order does not matter
     uint64_t n_queue = 0, n_upd = 0, n_active = 0, rounds = 0, integrated = 0;
     bool values_set = false;
     std::string err;
@@ -371,7 +414,7 @@ int order_device(foort_dmesh* m, uint64_t n_new, uint64_t& k) {
     if (n_new)
         DM_CK(cudaMemcpyAsync(m->active + m->n_active, m->newact, n_new * sizeof(ActiveSq), cudaMemcpyDeviceToDevice,
                               m->st));
-    if (n > 1) {
+    if (n > 1 && !(m->unordered && m->iteration >= n)) {
         size_t bytes = 0;
         DM_CK(cub::DeviceMergeSort::SortKeysCopy(nullptr, bytes, m->active, m->active_tmp, static_cast<int64_t>(n),
                                                  DeviceOrder(), m->st));
@@ -391,6 +434,17 @@ int order_device(foort_dmesh* m, uint64_t n_new, uint64_t& k) {
         std::swap(m->active, m->active_tmp);
     }
     m->n_active = n - k;
+    return FOORT_OK;
+}
+
+// Cells in ascending order (in and out distinct).
+int sort_cells(foort_dmesh* m, const uint64_t* in, uint64_t* out, uint64_t n) {
+    if (n == 0) return FOORT_OK;
+    size_t bytes = 0;
+    DM_CK(cub::DeviceRadixSort::SortKeys(nullptr, bytes, in, out, static_cast<int64_t>(n), 0, 64, m->st));
+    const int rc = ensure_tmp(m, bytes);
+    if (rc) return rc;
+    DM_CK(cub::DeviceRadixSort::SortKeys(m->tmp, bytes, in, out, static_cast<int64_t>(n), 0, 64, m->st));
     return FOORT_OK;
 }
 
@@ -426,6 +480,7 @@ int foort_dmesh_create_v2(uint64_t max_pixels, uint64_t initial_pixels, int32_t 
     foort_dmesh* m = new foort_dmesh();
     m->R = static_cast<uint64_t>(Rd);
     m->initial = n * n;
+    m->initial_arg = initial_pixels;
     m->iteration = iteration_pixels;
     m->max_pixels = max_pixels;
     m->left_px = max_pixels;
@@ -577,11 +632,201 @@ void foort_dmesh_destroy(foort_dmesh* m) {
     delete m;
 }
 
+}  // extern "C"
+
+// engine.cu (internal)
+extern "C" {
+uint32_t foort_ctx_schedule(const foort_ctx* ctx);
+uint64_t foort_ctx_budget(const foort_ctx* ctx);
+uint64_t foort_ctx_lookahead(const foort_ctx* ctx);
+void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule);
+}
+
+namespace {
+
+// Results of a run's pixels on the device: slot[cell] indexes pool (kNoSlot: none yet).
+struct DevStore {
+    uint32_t* slot = nullptr;
+    foort_result* pool = nullptr;
+    uint64_t cap = 0, used = 0;
+    uint64_t* list = nullptr;  // launch list (cells) and its scratch
+    uint64_t* sorted = nullptr;
+    uint8_t* flag = nullptr;
+    foort_pixel* px = nullptr;
+    uint64_t cap_list = 0;
+};
+
+void free_store(DevStore& S, cudaStream_t st) {
+    void* ptrs[] = {S.slot, S.pool, S.list, S.sorted, S.flag, S.px};
+    for (void* p : ptrs)
+        if (p) cudaFreeAsync(p, st);
+    cudaStreamSynchronize(st);
+}
+
+// Room for `need` more results in the pool, keeping those stored.
+int grow_pool(foort_dmesh* m, DevStore& S, uint64_t need) {
+    if (S.used + need <= S.cap && S.pool) return FOORT_OK;
+    const uint64_t cap = std::max<uint64_t>(S.used + need, 2 * S.cap);
+    if (cap >= kNoSlot) {
+        m->err = "too many results for 32-bit slots";
+        return FOORT_E_BADARG;
+    }
+    foort_result* p = nullptr;
+    DM_CK(cudaMallocAsync(reinterpret_cast<void**>(&p), cap * sizeof(foort_result), m->st));
+    if (S.used) DM_CK(cudaMemcpyAsync(p, S.pool, S.used * sizeof(foort_result), cudaMemcpyDeviceToDevice, m->st));
+    if (S.pool) DM_CK(cudaFreeAsync(S.pool, m->st));
+    S.pool = p;
+    S.cap = cap;
+    return FOORT_OK;
+}
+
+int grow_list(foort_dmesh* m, DevStore& S, uint64_t need) {
+    if (S.list && need <= S.cap_list) return FOORT_OK;
+    uint64_t c1 = S.list ? S.cap_list : 0, c2 = c1, c3 = c1, c4 = c1;
+    int rc = grow(m, S.list, c1, need, "cudaMallocAsync(launch list)");
+    if (!rc) rc = grow(m, S.sorted, c2, c1, "cudaMallocAsync(launch list)");
+    if (!rc) rc = grow(m, S.flag, c3, c1, "cudaMallocAsync(launch list)");
+    if (!rc) rc = grow(m, S.px, c4, c1, "cudaMallocAsync(launch list)");
+    S.cap_list = rc ? 0 : c1;
+    return rc;
+}
+
+// Integrate the cells of S.list[0, n) of image `image` (one launch) and store the results.
+int launch_cells(foort_ctx* ctx, foort_dmesh* m, DevStore& S, uint64_t n, uint32_t& launches) {
+    int rc = grow_pool(m, S, n);
+    if (rc) return rc;
+    k_cells_to_pixels<<<grid_for(n), 256, 0, m->st>>>(S.list, n, m->R, m->image, S.px);
+    DM_CK(cudaGetLastError());
+    if ((rc = foort_gpu_integrate_async(ctx, S.px, n, S.pool + S.used, m->st))) return rc;
+    ++launches;
+    if ((rc = foort_gpu_sync(ctx))) return rc;
+    k_set_slots<<<grid_for(n), 256, 0, m->st>>>(S.list, n, static_cast<uint32_t>(S.used), S.slot);
+    DM_CK(cudaGetLastError());
+    S.used += n;
+    return FOORT_OK;
+}
+
+// The queued cells of `q` without a result, compacted into S.list; returns the count.
+int unstored(foort_dmesh* m, DevStore& S, const uint64_t* q, uint64_t nq, uint64_t& n) {
+    n = 0;
+    if (!nq) return FOORT_OK;
+    int rc = grow_list(m, S, nq);
+    if (rc) return rc;
+    k_flag_unstored<<<grid_for(nq), 256, 0, m->st>>>(q, nq, S.slot, S.flag);
+    DM_CK(cudaGetLastError());
+    if ((rc = select_flagged(m, q, S.flag, S.list, m->num + 3, nq))) return rc;
+    long long h[4];
+    if ((rc = fetch(m, h, 3, 1))) return rc;
+    n = static_cast<uint64_t>(h[3]);
+    return FOORT_OK;
+}
+
+// The wave schedule: the level waves of a copy of `m` with unlimited IterationPixels, each
+// launch also taking the next wave's candidates while it stays within the lookahead cap;
+// then m's own rounds, each with its results gathered from the store.
+int run_dmesh_waves(foort_ctx* ctx, foort_dmesh* m, foort_result* d_out, uint64_t cap_out,
+                    foort_dmesh_round_fn on_round, void* user, uint64_t& total, uint32_t& nr, uint32_t& launches) {
+    foort_dmesh* w = nullptr;
+    int rc = foort_dmesh_create_v2(0, m->initial_arg, m->max_sub, UINT64_MAX, 0, FOORT_DIAG_FOUR_COLOR_SCREEN,
+                                   FOORT_DIAG_FOUR_COLOR_SCREEN, m->image, FOORT_DMESH_ORDER_DEVICE, m->st, &w);
+    if (rc) return rc;
+    w->value_diag = m->value_diag;
+    w->value_kind = m->value_kind;
+    w->unordered = true;
+    DevStore S;
+    auto done = [&](int code) {
+        free_store(S, m->st);
+        foort_dmesh_destroy(w);
+        return code;
+    };
+    const uint64_t cells = m->R * m->R, ahead = foort_ctx_lookahead(ctx);
+    uint64_t c0 = 0;
+    if ((rc = grow(m, S.slot, c0, cells, "cudaMallocAsync(slots)"))) return done(rc);
+    DM_CK(cudaMemsetAsync(S.slot, 0xFF, cells * sizeof(uint32_t), m->st));
+    while (w->n_queue) {
+        // every list of this wave in one allocation round: the launch list holds the wave's
+        // cells without a result and then at most nc candidates; the scratch list holds
+        // the nc raw candidates and their compaction
+        const uint64_t nc = ahead > 0 ? 5 * w->n_upd : 0;
+        if ((rc = grow_list(m, S, std::max<uint64_t>(w->n_queue + nc, 2 * nc)))) return done(rc);
+        uint64_t n = 0;
+        if ((rc = unstored(m, S, w->qcells, w->n_queue, n))) return done(rc);
+        if (n) {
+            const uint64_t n_todo = n;
+            if (ahead > n_todo && nc) {
+                // candidates: 5 per updating pixel, those without a result, each once
+                uint64_t* raw = S.sorted;       // nc raw candidates, later their sorted copy
+                uint64_t* kept = S.sorted + nc;  // those without a result
+                k_candidates<<<grid_for(w->n_upd), 256, 0, m->st>>>(w->upd, w->n_upd, w->level, S.slot, m->R,
+                                                                    m->max_sub, raw, S.flag);
+                DM_CK(cudaGetLastError());
+                if ((rc = select_flagged(m, raw, S.flag, kept, m->num + 3, nc))) return done(rc);
+                long long h[4];
+                if ((rc = fetch(m, h, 3, 1))) return done(rc);
+                const uint64_t nf = static_cast<uint64_t>(h[3]);
+                if (nf) {  // neighbouring squares share edge midpoints: each cell once
+                    if ((rc = sort_cells(m, kept, raw, nf))) return done(rc);
+                    size_t bytes = 0;
+                    DM_CK(cub::DeviceSelect::Unique(nullptr, bytes, raw, S.list + n_todo, m->num + 3,
+                                                    static_cast<int64_t>(nf), m->st));
+                    if ((rc = ensure_tmp(m, bytes))) return done(rc);
+                    DM_CK(cub::DeviceSelect::Unique(m->tmp, bytes, raw, S.list + n_todo, m->num + 3,
+                                                    static_cast<int64_t>(nf), m->st));
+                    if ((rc = fetch(m, h, 3, 1))) return done(rc);
+                    if (n_todo + static_cast<uint64_t>(h[3]) <= ahead) n = n_todo + static_cast<uint64_t>(h[3]);
+                }
+            }
+            if ((rc = launch_cells(ctx, m, S, n, launches))) return done(rc);
+        }
+        k_values_from_pool<<<grid_for(w->n_queue), 256, 0, m->st>>>(w->qcells, w->n_queue, S.slot, S.pool,
+                                                                     w->value_kind, w->value);
+        DM_CK(cudaGetLastError());
+        w->values_set = true;
+        if ((rc = foort_dmesh_end_current_loop(w))) {
+            m->err = w->err;
+            return done(rc);
+        }
+    }
+    // m's rounds from the store
+    while (m->n_queue) {
+        const uint64_t n = m->n_queue;
+        if (n > cap_out) {
+            m->err = "the result buffer holds " + std::to_string(cap_out) + " results, the round has " +
+                     std::to_string(n);
+            return done(FOORT_E_BADARG);
+        }
+        uint64_t miss = 0;
+        if ((rc = unstored(m, S, m->qcells, n, miss))) return done(rc);
+        if (miss && (rc = launch_cells(ctx, m, S, miss, launches))) return done(rc);
+        k_gather<<<grid_for(n), 256, 0, m->st>>>(m->qcells, n, S.slot, S.pool, d_out);
+        DM_CK(cudaGetLastError());
+        DM_CK(cudaStreamSynchronize(m->st));
+        if (on_round && (rc = on_round(user, m->qpx, d_out, n, nr))) return done(rc);
+        if ((rc = foort_dmesh_set_results(m, d_out, n))) return done(rc);
+        if ((rc = foort_dmesh_end_current_loop(m))) return done(rc);
+        total += n;
+        ++nr;
+    }
+    return done(FOORT_OK);
+}
+
+}  // namespace
+
+extern "C" {
+
 int foort_gpu_run_dmesh(foort_ctx* ctx, foort_dmesh* m, foort_result* d_out, uint64_t cap_out,
                         foort_dmesh_round_fn on_round, void* user, uint64_t* geodesics, uint32_t* rounds) {
     if (!ctx || !m || !d_out) return FOORT_E_BADARG;
     uint64_t total = 0;
-    uint32_t nr = 0;
+    uint32_t nr = 0, launches = 0;
+    if (foort_ctx_schedule(ctx) == FOORT_SCHEDULE_WAVES && m->infinite && m->rounds == 0 && foort_ctx_budget(ctx) == 0) {
+        const int rc = run_dmesh_waves(ctx, m, d_out, cap_out, on_round, user, total, nr, launches);
+        foort_ctx_set_run_info(ctx, launches, FOORT_SCHEDULE_WAVES);
+        if (rc) return rc;
+        if (geodesics) *geodesics = total;
+        if (rounds) *rounds = nr;
+        return FOORT_OK;
+    }
     while (m->n_queue) {
         const uint64_t n = m->n_queue;
         if (n > cap_out) {
@@ -591,6 +836,8 @@ int foort_gpu_run_dmesh(foort_ctx* ctx, foort_dmesh* m, foort_result* d_out, uin
         }
         int rc = foort_gpu_integrate_async(ctx, m->qpx, n, d_out, m->st);
         if (rc) return rc;
+        ++launches;
+        foort_ctx_set_run_info(ctx, launches, FOORT_SCHEDULE_ROUNDS);
         if ((rc = foort_gpu_sync(ctx))) return rc;
         if (on_round && (rc = on_round(user, m->qpx, d_out, n, nr))) return rc;
         if ((rc = foort_dmesh_set_results(m, d_out, n))) return rc;
@@ -598,6 +845,7 @@ int foort_gpu_run_dmesh(foort_ctx* ctx, foort_dmesh* m, foort_result* d_out, uin
         total += n;
         ++nr;
     }
+    foort_ctx_set_run_info(ctx, launches, FOORT_SCHEDULE_ROUNDS);
     if (geodesics) *geodesics = total;
     if (rounds) *rounds = nr;
     return FOORT_OK;

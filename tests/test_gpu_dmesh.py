@@ -148,10 +148,13 @@ def test_device_order_with_ties_is_a_valid_subdivision(eng):
             assert np.array_equal(np.sort(ca), np.sort(cells))
 
 
-def test_run_dmesh_matches_the_host_round_loop(eng):
+@pytest.mark.parametrize("schedule,lookahead", [(abi.SCHEDULE_WAVES, None), (abi.SCHEDULE_WAVES, 0),
+                                                (abi.SCHEDULE_ROUNDS, None)])
+def test_run_dmesh_matches_the_host_round_loop(eng, schedule, lookahead):
     """foort_gpu_run_dmesh over a Kerr a = 0.99 V2 run (33^2 seed, MaxSubdivide 3,
     IterationPixels 150): each round's pixels and results equal those of the host loop
-    (host mesh, foort_gpu_integrate) bit for bit."""
+    (host mesh, foort_gpu_integrate) bit for bit, whether the device run launches round by
+    round or by level waves (at most three launches, fewer with lookahead)."""
     import torch
     wl = workloads.c2(abi.PREC_MIXED)
     spec = dict(max_pixels=0, initial_pixels=33 * 33, max_subdivide=3, iteration_pixels=150,
@@ -177,8 +180,16 @@ def test_run_dmesh_matches_the_host_round_loop(eng):
             dev_rounds.append((dmesh.pixels(), res))
             assert d_res == out.data_ptr() and d_px == dmesh.pixels_ptr() and rnd == len(dev_rounds) - 1
 
+        e.set_schedule(schedule)
+        e.set_lookahead(lookahead)
         g, r = dmesh.run(e, out.data_ptr(), cap, on_round)
+        launches, used = e.run_info()
     assert r == len(host_rounds) == len(dev_rounds) >= 3
+    assert used == schedule
+    if schedule == abi.SCHEDULE_ROUNDS:
+        assert launches == r
+    else:  # three levels; with lookahead the second launch also holds the third level
+        assert launches <= (3 if lookahead == 0 else 2)
     assert g == sum(len(p) for p, _ in host_rounds)
     for k, ((hp, hr), (dp, dr)) in enumerate(zip(host_rounds, dev_rounds)):
         assert np.array_equal(hp, dp), k

@@ -48,7 +48,7 @@ def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision, s
         assert launches == rounds
         assert sum(len(p) for p in launched) == geodesics
     else:
-        assert launches <= min(3, rounds)  # MaxSubdivide 3
+        assert launches <= min(3 if lookahead == 0 else 2, rounds)  # MaxSubdivide 3
         assert sum(len(p) for p in launched) >= geodesics
         if lookahead == 0:
             assert sum(len(p) for p in launched) == geodesics
