@@ -106,6 +106,8 @@ def load():
     lib.foort_tune_load.argtypes = [C.c_char_p]
     lib.foort_mesh_create_waves.argtypes = [vp, C.POINTER(vp)]
     lib.foort_mesh_lookahead.argtypes = [vp, u32, vp, u64, C.POINTER(u64)]
+    lib.foort_mesh_max_pixels.argtypes = [vp]
+    lib.foort_mesh_max_pixels.restype = u64
     lib.foort_gpu_set_lookahead.argtypes = [vp, u64]
     lib.foort_gpu_set_record_launches.argtypes = [vp, i32]
     lib.foort_gpu_run_launch.argtypes = [vp, u32, vp, u64, C.POINTER(u64)]
@@ -411,6 +413,10 @@ class Mesh:
     def end_round(self):
         self._lib.foort_mesh_end_current_loop(self._m)
 
+    def max_pixels(self):
+        """Most pixels the mesh hands out over a run (0: no limit)."""
+        return self._lib.foort_mesh_max_pixels(self._m)
+
     def lookahead(self, image=0):
         """foort_mesh_lookahead: candidates of the next round of a mesh of level waves."""
         n = C.c_uint64()
@@ -679,20 +685,46 @@ def _pixel_keys(px):
 
 
 def run_by_waves(mesh_specs, desc, integrate, on_round=None):
-    """foort_gpu_run's level-wave schedule with any integrate(px) -> results: the meshes'
-    level waves (Mesh.waves) are integrated first, one integrate() call per wave, then the
-    meshes' rounds are replayed from the stored results, so on_round(px, res) sees the
-    reference's rounds. A round's pixels that no wave held (none, for meshes that have
-    waves) go to integrate() then. Returns (rounds, integrate calls)."""
+    """foort_gpu_run's level-wave schedule (without lookahead) with any integrate(px) ->
+    results: the meshes' level waves (Mesh.waves) are integrated first, one integrate()
+    call per wave, an image's waves stopping before the one that would take them past its
+    mesh's max_pixels; then the meshes' rounds are replayed from the stored results, so
+    on_round(px, res) sees the reference's rounds. A round's pixels that no wave held go
+    to integrate() then. Returns (rounds, integrate calls)."""
     keys, results = [], []
-
-    def wave(px):
-        res = integrate(px)
-        keys.append(_pixel_keys(px))
-        results.append(res)
-        return res
-
-    calls = run_rounds(mesh_specs, desc, wave, waves=True)
+    meshes = [Mesh.from_spec(spec, desc.diag_flags, desc.value_diag) for spec in mesh_specs]
+    waves = []
+    for m in meshes:
+        waves.append(m.waves())
+        budget = m.max_pixels()
+        waves[-1].budget = budget if budget else float("inf")
+        waves[-1].handed = 0
+        m.close()
+    calls = 0
+    try:
+        while True:
+            live = []
+            for i, w in enumerate(waves):
+                if w.finished() or w.size() > w.budget - w.handed:
+                    continue
+                live.append((i, w))
+            if not live:
+                break
+            parts = [w.pixels(image=i) for i, w in live]
+            px = np.concatenate(parts)
+            res = integrate(px)
+            calls += 1
+            keys.append(_pixel_keys(px))
+            results.append(res)
+            k = 0
+            for (i, w), p in zip(live, parts):
+                w.handed += len(p)
+                w.set_results(res[k:k + len(p)])
+                w.end_round()
+                k += len(p)
+    finally:
+        for w in waves:
+            w.close()
     k = np.concatenate(keys) if keys else np.zeros(0, np.int64)
     r = np.concatenate(results) if results else np.zeros(0, abi.RESULT_DTYPE)
     order = np.argsort(k, kind="stable")

@@ -70,6 +70,8 @@ struct foort_mesh {
     // Every pixel the next round could hand out: the five candidates of each square that
     // awaits its weight (foort_mesh_lookahead); cells, each once.
     virtual void lookahead(std::vector<uint64_t>&) const {}
+    // Most pixels the mesh hands out over a run (0: no limit).
+    virtual uint64_t pixel_cap() const = 0;
 };
 
 namespace {
@@ -91,6 +93,7 @@ struct SimpleMesh final : foort_mesh {
     std::string description() const override {
         return "Mesh: simple square grid (" + std::to_string(grid) + "^2 pixels)";
     }
+    uint64_t pixel_cap() const override { return total; }
     foort_mesh* wave_clone() const override {
         if (fin) return nullptr;
         auto* m = new SimpleMesh(*this);
@@ -250,9 +253,10 @@ struct V2Mesh final : foort_mesh {
     // positive weight is left, so every such square is subdivided in some round: the
     // run's pixel set is fixed by the values alone, and IterationPixels only spreads it
     // over rounds. With IterationPixels unlimited, round k hands out the pixels of
-    // subdivision level k.
+    // subdivision level k. The copy is unlimited also where this mesh is not: its pixels
+    // then hold this mesh's (at most MaxPixels of them, cut in the round order).
     foort_mesh* wave_clone() const override {
-        if (!infinite || n_rounds != 0) return nullptr;
+        if (n_rounds != 0) return nullptr;
         auto* m = new V2Mesh();
         m->kind = kind;
         m->grid = grid;
@@ -269,6 +273,7 @@ struct V2Mesh final : foort_mesh {
     // The squares of the updating list get their weights at the end of this round; the
     // next round subdivides some of them (all that get a positive weight, in a wave mesh),
     // and each subdivision hands out at most its square's p2, p4, p5, p6 and p8.
+    uint64_t pixel_cap() const override { return infinite ? 0 : max_pixels; }
     void lookahead(std::vector<uint64_t>& cells) const override {
         cells.clear();
         cells.reserve(5 * updating.size());
@@ -393,6 +398,8 @@ int foort_mesh_end_current_loop(foort_mesh* m) {
 }
 
 void foort_mesh_destroy(foort_mesh* m) { delete m; }
+
+uint64_t foort_mesh_max_pixels(const foort_mesh* m) { return m ? m->pixel_cap() : 0; }
 
 int foort_mesh_lookahead(const foort_mesh* m, uint32_t image, foort_pixel* out, uint64_t cap, uint64_t* n) {
     if (!m || !n) return FOORT_E_BADARG;

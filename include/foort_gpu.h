@@ -422,15 +422,20 @@ int foort_mesh_end_current_loop(foort_mesh* mesh);
 
 void foort_mesh_destroy(foort_mesh* mesh);
 
-/* The mesh's level waves: a new, unstarted mesh with the same parameters whose rounds
- * subdivide every square of positive weight (IterationPixels unlimited), so that its
- * round k hands out the pixels of subdivision level k. For a SquareSubdivisionMeshV2 with
- * unlimited MaxPixels (0) the reference's rounds go on until no square of positive weight
- * is left, so both meshes hand out the same pixels, the waves in max_subdivide rounds or
- * fewer; a SimpleSquareMesh is its own single wave. FOORT_E_UNSUPPORTED for a V2 mesh
- * with a finite MaxPixels (the cut depends on the round order) and for a mesh that has
- * ended a round. Engine extension: the reference has no such schedule. */
+/* The mesh's level waves: a new, unstarted mesh with the same parameters but unlimited
+ * IterationPixels and MaxPixels, whose rounds subdivide every square of positive weight,
+ * so that its round k hands out the pixels of subdivision level k. For a
+ * SquareSubdivisionMeshV2 with unlimited MaxPixels (0) the reference's rounds go on until
+ * no square of positive weight is left, so both meshes hand out the same pixels, the
+ * waves in max_subdivide rounds or fewer; with a finite MaxPixels the mesh hands out at
+ * most that many of the waves' pixels (the cut depends on the round order). A
+ * SimpleSquareMesh is its own single wave. FOORT_E_UNSUPPORTED for a mesh that has ended
+ * a round. Engine extension: the reference has no such schedule. */
 int foort_mesh_create_waves(const foort_mesh* mesh, foort_mesh** out);
+
+/* The most pixels the mesh hands out over a run: MaxPixels of a V2 mesh (0: unlimited),
+ * the grid's pixel count of a SimpleSquareMesh. */
+uint64_t foort_mesh_max_pixels(const foort_mesh* mesh);
 
 /* The pixels that the squares whose weight the end of this round decides can add: the top
  * and left edge midpoints, the centre and the right and bottom edge midpoints of each, as
@@ -581,13 +586,14 @@ int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const
 
 /* Schedule of foort_gpu_run's launches. Engine extension: the reference integrates
  * round after round (Main.cpp:313-419).
- *   FOORT_SCHEDULE_WAVES (default): where every mesh has level waves
- *     (foort_mesh_create_waves), no step budget is set and GeodesicPosition is off, the
- *     run integrates the waves -- one launch per subdivision level, over all images --
- *     and then replays the meshes' rounds from the stored results. The meshes, the output
- *     files and the returned counts see the reference's rounds in the reference's order,
- *     and each result is the one the round's own launch would give (a geodesic's result
- *     does not depend on the launch it runs in). A pixel of a round that no wave held is
+ *   FOORT_SCHEDULE_WAVES (default): where no step budget is set and GeodesicPosition is
+ *     off, the run integrates the meshes' level waves (foort_mesh_create_waves) -- one
+ *     launch per subdivision level, over all images -- and then replays the meshes'
+ *     rounds from the stored results. The meshes, the output files and the returned
+ *     counts see the reference's rounds in the reference's order, and each result is the
+ *     one the round's own launch would give (a geodesic's result does not depend on the
+ *     launch it runs in). An image's waves stop before the one that would take its
+ *     pixels past foort_mesh_max_pixels. A pixel of a round that no wave held is
  *     integrated then, in one launch per such round. Elsewhere the run goes round by round.
  *   FOORT_SCHEDULE_ROUNDS: one launch per round.
  * foort_gpu_run_info reports the last run's launch count and the schedule it used. */

@@ -112,3 +112,34 @@ def test_run_records_the_reference_positions(engine_lib, tmp_path, name, precisi
     frac = 1.0 if precision == abi.PREC_FP64 else 0.99
     print(f"{name}: {len(same)}/{len(ref_order)} same counts, {ok.mean():.5f} of those geodesics within {tol}")
     assert ok.mean() >= frac
+
+
+@pytest.mark.parametrize("max_pixels", [400, 700, 100000])
+def test_wave_schedule_under_a_pixel_budget_writes_the_round_files(engine_lib, tmp_path, max_pixels):
+    """A V2 run (17^2 seed, MaxSubdivide 3, IterationPixels 150) whose MaxPixels cuts the
+    rounds (400, 700) or never does (100000): the wave schedule, which stops an image's
+    waves at its budget and integrates what the rounds then miss, writes the same files as
+    the round-by-round schedule, byte for byte."""
+    import foort_gb300
+    wl = workloads.johannsen_golden(True, precision=abi.PREC_MIXED)
+    spec = ("v2", dict(max_pixels=max_pixels, initial_pixels=17 * 17, max_subdivide=3, iteration_pixels=150))
+    files, counts = {}, {}
+    for schedule in (abi.SCHEDULE_ROUNDS, abi.SCHEDULE_WAVES):
+        d = tmp_path / str(schedule)
+        d.mkdir()
+        mesh = foort_gb300.Mesh.from_spec(spec, wl.desc.diag_flags, wl.desc.value_diag)
+        out = foort_gb300.Output(str(d / "run"), wl.desc.diag_flags, wl.desc.value_diag,
+                                 first_line=mesh.first_line_info(wl.desc))
+        with foort_gb300.Engine(wl.desc) as e:
+            e.set_schedule(schedule)
+            counts[schedule] = e.run([mesh], [out]) + e.run_info()
+        out.close()
+        mesh.close()
+        files[schedule] = {f.name: f.read_bytes() for f in sorted(d.iterdir())}
+    assert files[abi.SCHEDULE_WAVES] == files[abi.SCHEDULE_ROUNDS] and files[abi.SCHEDULE_ROUNDS]
+    g_r, r_r, l_r, s_r = counts[abi.SCHEDULE_ROUNDS]
+    g_w, r_w, l_w, s_w = counts[abi.SCHEDULE_WAVES]
+    assert (g_w, r_w) == (g_r, r_r) and g_r <= max_pixels
+    assert (s_r, s_w) == (abi.SCHEDULE_ROUNDS, abi.SCHEDULE_WAVES) and l_r == r_r
+    if max_pixels == 100000:
+        assert l_w < l_r
