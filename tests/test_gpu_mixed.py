@@ -127,10 +127,10 @@ def c2_sample(n=8000, seed=11):
 # points within 1e-6 and the median within 1e-7; a backward error (error / kappa, in units
 # of the screen) with p99 within 1e-6 and a median no larger than that of the plain FP64
 # kernel, whose finite differences (h = 1e-7) keep fewer digits where the metric is nearly
-# flat. In log-r mode the FP32 rounding of the coordinate term -(u^1)^2, ~1000 times the
-# physical radial acceleration at r = 1000, costs ~1e-7 of u^1 per evaluation: there the
-# median within 1e-6, 80 % of well-conditioned pixels within 1e-6 and the backward error's
-# p99 within 1e-6.
+# flat. In log-r mode the backward error is as small as in plain r, but the reference's
+# finite differences are far better there (h = 1e-7 in ln r is a relative step) and the
+# shipped log-r view is mostly ill-conditioned pixels: there the median within 1e-6, 80 %
+# of well-conditioned pixels within 1e-6 and the backward error's p99 within 1e-6.
 ORACLE_CASES = dict(CASES, c2_sample8000=None)
 
 
