@@ -74,6 +74,9 @@ DRAM_BYTES_PER_GEODESIC = {("kerr", "rk4"): 121.1}
 # 4 x 152 sub-partitions) they give the fraction of issue slots the path fills.
 EXEC_INSTR_PER_STEP = {("kerr", "rk4", 2): 2000, ("kerr", "rk4", 1): 1320}
 SUBPARTITIONS = 4
+# runs of more geodesics take the FP64 legs on a seeded sample (1 %, at least 20,000)
+FP64_SAMPLE_ABOVE = 60000
+FP64_SAMPLE_SEED = 20261203
 
 
 from foort_gb300.multirank import dist_env  # noqa: E402
@@ -552,7 +555,7 @@ def main():
     # ---- the same pixels launched round by round (the reference's rounds), device-resident;
     # sizes the search has not seen are tuned in the warm-up
     rounds_leg = None
-    if launches_px is not rounds:
+    if [len(r) for r in launches_px] != [len(r) for r in rounds]:
         r_lists = to_device(rounds) + (rounds,)
         with foort_gb300.Engine(wl.desc) as e:
             e.set_lanes(args.lanes)
@@ -683,10 +686,33 @@ def main():
                           "device, results left in device memory"}
 
     # ---- FP64 plain kernel on the same pixels (N = 1 only: under torchrun the other GPUs
-    # would wait for it)
+    # would wait for it). Runs of more than FP64_SAMPLE_ABOVE geodesics (C3, C4, C5) take
+    # the FP64 legs on a seeded sample of their pixels instead: 1 %, at least 20,000.
     fp64 = None
     acc = None
-    if not args.no_fp64 and world == 1:
+    if not args.no_fp64 and world == 1 and n_geod > FP64_SAMPLE_ABOVE:
+        run_px = np.concatenate(rounds)
+        rng = np.random.default_rng(FP64_SAMPLE_SEED)
+        n_s = min(n_geod, max(20000, n_geod // 100))
+        sample = run_px[np.sort(rng.choice(n_geod, n_s, replace=False))]
+        rates, res_s = {}, {}
+        for prec in (abi.PREC_MIXED, abi.PREC_FP64):
+            wls = workload(args.workload, prec, args.iteration_pixels)
+            with foort_gb300.Engine(wls.desc) as e:
+                e.set_lanes(args.lanes)
+                e.integrate(sample[:256])  # warm-up
+                res_s[prec] = e.integrate(sample)
+                st = e.stats()
+            rates[prec] = (n_s / (st["kernel_ms"] * 1e-3), st["kernel_ms"], st["steps"])
+        r64, t64, steps64 = rates[abi.PREC_FP64]
+        fp64 = {"value": r64, "unit": UNIT, "ms_per_step": t64, "steps_per_s": steps64 / (t64 * 1e-3),
+                "sample": f"{n_s} seeded-random pixels of the run's {n_geod}, one launch per kernel",
+                "mixed_on_sample": rates[abi.PREC_MIXED][0],
+                "roofline_fp64": {"achieved": steps64 * OPS_PER_STEP.get(mkind, 1130) / (t64 * 1e-3) / 1e12,
+                                  "peak": peaks[1], "unit": "TFLOP/s",
+                                  "frac": steps64 * OPS_PER_STEP.get(mkind, 1130) / (t64 * 1e-3) / 1e12 / peaks[1]}}
+        acc = accuracy_legs(foort_gb300, args, wl, sample, res_s[abi.PREC_MIXED], res_s[abi.PREC_FP64])
+    elif not args.no_fp64 and world == 1:
         wl64 = workload(args.workload, abi.PREC_FP64, args.iteration_pixels)
         with foort_gb300.Engine(wl64.desc) as e:
             e.integrate(rounds[-1][:256])  # warm-up
@@ -784,7 +810,9 @@ def main():
         "gpu_launches": args.steps * len(launches_px),
         "e2e": e2e, "e2e_per_round_api": e2e_rounds, "rounds_schedule": rounds_leg, "device_mesh": dmesh,
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-        "fp64": fp64, "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
+        "fp64": fp64,
+        "speedup_vs_fp64": ((fp64["mixed_on_sample"] if "sample" in fp64 else value / world) / fp64["value"])
+        if fp64 else None,
         "accuracy": acc,
         "round_sizes": [len(r) for r in rounds],
         "launch_sizes": [len(r) for r in launches_px],

@@ -108,6 +108,7 @@ def load():
     lib.foort_mesh_lookahead.argtypes = [vp, u32, vp, u64, C.POINTER(u64)]
     lib.foort_mesh_max_pixels.argtypes = [vp]
     lib.foort_mesh_max_pixels.restype = u64
+    lib.foort_mesh_kind.argtypes = [vp]
     lib.foort_gpu_set_lookahead.argtypes = [vp, u64]
     lib.foort_gpu_set_record_launches.argtypes = [vp, i32]
     lib.foort_gpu_run_launch.argtypes = [vp, u32, vp, u64, C.POINTER(u64)]

@@ -400,6 +400,7 @@ int foort_mesh_end_current_loop(foort_mesh* m) {
 void foort_mesh_destroy(foort_mesh* m) { delete m; }
 
 uint64_t foort_mesh_max_pixels(const foort_mesh* m) { return m ? m->pixel_cap() : 0; }
+int foort_mesh_kind(const foort_mesh* m) { return m ? m->kind : FOORT_E_BADARG; }
 
 int foort_mesh_lookahead(const foort_mesh* m, uint32_t image, foort_pixel* out, uint64_t cap, uint64_t* n) {
     if (!m || !n) return FOORT_E_BADARG;

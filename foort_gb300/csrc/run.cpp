@@ -268,7 +268,11 @@ int run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs,
     int rc = FOORT_OK;
     ResultStore store;
     schedule = FOORT_SCHEDULE_ROUNDS;
-    if (foort_ctx_schedule(ctx) == FOORT_SCHEDULE_WAVES && !geopos && foort_ctx_budget(ctx) == 0) {
+    // A SimpleSquareMesh is its own single wave: without an adaptive mesh the waves are
+    // the rounds, and storing the results would only cost time.
+    bool adaptive = false;
+    for (uint32_t i = 0; i < n_images; ++i) adaptive = adaptive || foort_mesh_kind(meshes[i]) == FOORT_MESH_SUBDIVISION_V2;
+    if (adaptive && foort_ctx_schedule(ctx) == FOORT_SCHEDULE_WAVES && !geopos && foort_ctx_budget(ctx) == 0) {
         rc = integrate_waves(ctx, meshes, n_images, store, launches);
         if (rc == FOORT_OK) {
             schedule = FOORT_SCHEDULE_WAVES;

@@ -437,6 +437,11 @@ int foort_mesh_create_waves(const foort_mesh* mesh, foort_mesh** out);
  * the grid's pixel count of a SimpleSquareMesh. */
 uint64_t foort_mesh_max_pixels(const foort_mesh* mesh);
 
+/* FOORT_MESH_SIMPLE or FOORT_MESH_SUBDIVISION_V2. */
+#define FOORT_MESH_SIMPLE 0
+#define FOORT_MESH_SUBDIVISION_V2 1
+int foort_mesh_kind(const foort_mesh* mesh);
+
 /* The pixels that the squares whose weight the end of this round decides can add: the top
  * and left edge midpoints, the centre and the right and bottom edge midpoints of each, as
  * pixels of `image` in row-major order (V2 meshes; none for a SimpleSquareMesh). In a mesh
@@ -586,8 +591,9 @@ int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const
 
 /* Schedule of foort_gpu_run's launches. Engine extension: the reference integrates
  * round after round (Main.cpp:313-419).
- *   FOORT_SCHEDULE_WAVES (default): where no step budget is set and GeodesicPosition is
- *     off, the run integrates the meshes' level waves (foort_mesh_create_waves) -- one
+ *   FOORT_SCHEDULE_WAVES (default): where a mesh is a SquareSubdivisionMeshV2, no step
+ *     budget is set and GeodesicPosition is off, the run integrates the meshes' level
+ *     waves (foort_mesh_create_waves) -- one
  *     launch per subdivision level, over all images -- and then replays the meshes'
  *     rounds from the stored results. The meshes, the output files and the returned
  *     counts see the reference's rounds in the reference's order, and each result is the

@@ -43,7 +43,8 @@ def test_run_writes_the_reference_files(engine_lib, tmp_path, name, precision, s
     out.close()
     mesh.close()
     print(f"{name}: {geodesics} geodesics in {rounds} rounds, {launches} launches")
-    assert used == schedule and len(launched) == launches
+    # a SimpleSquareMesh is its own single wave: the run goes by rounds
+    assert used == (schedule if name.startswith("v2") else abi.SCHEDULE_ROUNDS) and len(launched) == launches
     if schedule == abi.SCHEDULE_ROUNDS or name.startswith("simple"):
         assert launches == rounds
         assert sum(len(p) for p in launched) == geodesics
