@@ -272,6 +272,7 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
     const unsigned slots = PAIR ? 0x55555555u : kFullMask;  // one bit per geodesic slot
     const unsigned pmask = 3u << (lane & ~1u);
     typename E::Lane L;
+    ImageConst Ic;  // PAIR: the lane's image constants in registers, copied at each refill
     bool active = false;
     bool drained = false;
     bool stopping = false;
@@ -308,6 +309,7 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                                        ? GeoposRec{A.gp_plan[my].dst, A.gp_plan[my].j, A.gp_plan[my].M, 0, 0}
                                        : GeoposRec{nullptr, 1, 0, 0, 0};
                             E::init(L, A.images[p.image], R, p);
+                            if constexpr (PAIR) Ic = A.images[p.image];
                             active = true;
                         }
                     }
@@ -321,12 +323,11 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
         // Integrate until a lane needs new work (while work remains) or a poll is due.
         for (;;) {
             if (active) {
-                const ImageConst& I = A.images[L.img];
                 bool more;
                 if constexpr (PAIR) {
-                    more = E::step_pair(L, I, R, odd, pmask);
+                    more = E::step_pair(L, Ic, R, odd, pmask);
                 } else {
-                    more = E::step(L, I, R);
+                    more = E::step(L, A.images[L.img], R);
                 }
                 if (!odd) ++lane_steps;
                 if (!more) {

@@ -319,6 +319,16 @@ __device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const Mixe
     return (h < hmin) ? hmin : h;
 }
 
+// DecideUpdate with a step counter, without branches: every == 0, or the counter
+// reaching every (and restarting).
+template <typename C>
+__device__ __forceinline__ bool decide_nb(uint64_t every, C& cnt) {
+    const C next = cnt + 1;
+    const bool hit = (every == 0) | (static_cast<uint64_t>(next) >= every);
+    cnt = (every == 0) ? cnt : (hit ? C(0) : next);
+    return hit;
+}
+
 // FOORT_MIXED_FP64_TURNING_POINTS: FP64 steps where the radial or the polar speed is
 // below this fraction of the ray's angular motion.
 constexpr float kTurningFraction = 0.05f;
@@ -436,13 +446,13 @@ struct MixedEngine {
             if (L.term == FOORT_TERMCODE_HORIZON) L.passes = -L.passes;
         }
         if (R.diag_flags & FOORT_DIAG_CLOSEST_RADIUS) {
-            if (diag_decide(R.cr_every, R.cr_start, R.cr_finish, L.cC, lamd, L.term)) {
-                // in log-r mode ln r is tracked (exp is monotonic) and exponentiated once
-                if (!L.has_rmin || ff_lt(L.x[1], L.rmin)) {
-                    L.rmin = L.x[1];
-                    L.has_rmin = true;
-                }
-            }
+            const bool d = (R.cr_every > 0) ? decide_nb(R.cr_every, L.cC)
+                                             : diag_decide(R.cr_every, R.cr_start, R.cr_finish, L.cC, lamd, L.term);
+            // in log-r mode ln r is tracked (exp is monotonic) and exponentiated once
+            const bool upd = d & (!L.has_rmin | ff_lt(L.x[1], L.rmin));
+            L.rmin.hi = upd ? L.x[1].hi : L.rmin.hi;
+            L.rmin.lo = upd ? L.x[1].lo : L.rmin.lo;
+            L.has_rmin = L.has_rmin | upd;
         }
     }
 
@@ -453,32 +463,32 @@ struct MixedEngine {
             return check_terms(R, I.m.rh, I.h_eps, r, ff_d(L.x[2]), L.T);
         }
         // Same order and cadence as check_terms; thresholds precomputed as float-float
-        // (in ln r in log-r mode).
-        if (R.term_flags & FOORT_TERM_HORIZON) {
-            if (term_decide(R.h_every, L.T.cH)) {
-                if (ff_lt(L.x[1], ff_of(I.mx.hthr)) || (I.m.rh == 0.0 && ff_lt(L.x[1], ff_of(I.mx.hthr0))))
-                    return FOORT_TERMCODE_HORIZON;
-            }
-        }
-        if (R.term_flags & FOORT_TERM_BOUNDARY_SPHERE) {
-            if (term_decide(R.b_every, L.T.cB)) {
-                if (ff_lt(ff_of(I.mx.bthr), L.x[1])) return FOORT_TERMCODE_BOUNDARY_SPHERE;
-            }
+        // (in ln r in log-r mode). Without branches: every termination's counter advances,
+        // and the checks run in reverse order so that the first in the reference's order
+        // wins (the reference stops at it, and a finished geodesic's counters are unused).
+        int code = FOORT_TERMCODE_CONTINUE;
+        if (R.term_flags & FOORT_TERM_THETA_SINGULARITY) {
+            const bool d = decide_nb(R.th_every, L.T.cTh);
+            const ff e = ff_of(I.mx.theps);
+            const bool hit = ff_lt(ff_abs(L.x[2]), e) | ff_lt(ff_abs(ff_add(ff_of(I.mx.pi), ff_neg(L.x[2]))), e);
+            code = (d & hit) ? FOORT_TERMCODE_THETA_SINGULARITY : code;
         }
         if (R.term_flags & FOORT_TERM_TIMEOUT) {
-            if (term_decide(R.t_every, L.T.cT)) {
-                if (L.T.tcur >= R.t_max) return FOORT_TERMCODE_TIMEOUT;
-                ++L.T.tcur;
-            }
+            const bool d = decide_nb(R.t_every, L.T.cT);
+            const bool hit = L.T.tcur >= R.t_max;
+            code = (d & hit) ? FOORT_TERMCODE_TIMEOUT : code;
+            L.T.tcur += (d & !hit) ? 1u : 0u;
         }
-        if (R.term_flags & FOORT_TERM_THETA_SINGULARITY) {
-            if (term_decide(R.th_every, L.T.cTh)) {
-                const ff e = ff_of(I.mx.theps);
-                if (ff_lt(ff_abs(L.x[2]), e) || ff_lt(ff_abs(ff_add(ff_of(I.mx.pi), ff_neg(L.x[2]))), e))
-                    return FOORT_TERMCODE_THETA_SINGULARITY;
-            }
+        if (R.term_flags & FOORT_TERM_BOUNDARY_SPHERE) {
+            const bool d = decide_nb(R.b_every, L.T.cB);
+            code = (d & ff_lt(ff_of(I.mx.bthr), L.x[1])) ? FOORT_TERMCODE_BOUNDARY_SPHERE : code;
         }
-        return FOORT_TERMCODE_CONTINUE;
+        if (R.term_flags & FOORT_TERM_HORIZON) {
+            const bool d = decide_nb(R.h_every, L.T.cH);
+            const bool hit = ff_lt(L.x[1], ff_of(I.mx.hthr)) | ((I.m.rh == 0.0) & ff_lt(L.x[1], ff_of(I.mx.hthr0)));
+            code = (d & hit) ? FOORT_TERMCODE_HORIZON : code;
+        }
+        return code;
     }
 
     // A right-hand side through the plugin's FP32 form (inlined or called).
