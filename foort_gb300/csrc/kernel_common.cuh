@@ -329,7 +329,7 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                 } else {
                     more = E::step(L, A.images[L.img], R);
                 }
-                if (!odd) ++lane_steps;
+                lane_steps += odd ? 0u : 1u;
                 if (!more) {
                     if (!odd) {
                         E::finish(L, R, &A.out[idx]);

@@ -420,30 +420,31 @@ struct MixedEngine {
     // the compensated state; FourColorScreen at termination (Diagnostics.cpp:159-200).
     static __device__ __forceinline__ void diags(Lane& L, const ImageConst& I, const RunConst& R, bool at_start) {
         const double lamd = at_start ? 0.0 : 1.0;  // only compared with 0 by DecideUpdate
-        if (R.diag_flags & FOORT_DIAG_FOUR_COLOR_SCREEN) {
-            if (L.term == FOORT_TERMCODE_BOUNDARY_SPHERE) L.quad = four_color_quadrant(ff_d(L.x[2]), ff_d(L.x[3]));
-        }
+        // FourColorScreen's quadrant and EquatorialPasses' sign at the Horizon are taken at
+        // termination from the final state, which no later step changes (write()).
         if (R.diag_flags & FOORT_DIAG_EQUATORIAL_PASSES) {
-            if (diag_decide(R.eq_every, R.eq_start, R.eq_finish, L.cE, lamd, L.term)) {
-                if (DECIDE64) {
+            if (DECIDE64) {
+                if (diag_decide(R.eq_every, R.eq_start, R.eq_finish, L.cE, lamd, L.term)) {
                     const double th = ff_d(L.x[2]);
                     if (fabs(th - kRefPi / 2.0) > kRefPi / 2.0 * R.eq_thr) {
                         const double pv = ff_d(L.prev);
                         if (pv > 0 && ((pv - kRefPi / 2.0) * (th - kRefPi / 2.0)) < 0.0) ++L.passes;
                         L.prev = L.x[2];
                     }
-                } else {
-                    const ff d = ff_add(L.x[2], ff_of(I.mx.mpio2));
-                    if (ff_lt(ff_of(I.mx.eqthr), ff_abs(d))) {
-                        if (L.prev.hi > 0.f) {
-                            const ff dprev = ff_add(L.prev, ff_of(I.mx.mpio2));
-                            if (ff_neg_sign(dprev) != ff_neg_sign(d)) ++L.passes;
-                        }
-                        L.prev = L.x[2];
-                    }
                 }
+            } else {
+                // without branches: a crossing counts where the sample is taken, theta is
+                // away from the equator and on the other side of it than the last sample
+                const bool d = (R.eq_every > 0) ? decide_nb(R.eq_every, L.cE)
+                                                 : diag_decide(R.eq_every, R.eq_start, R.eq_finish, L.cE, lamd, L.term);
+                const ff dt = ff_add(L.x[2], ff_of(I.mx.mpio2));
+                const bool upd = d & ff_lt(ff_of(I.mx.eqthr), ff_abs(dt));
+                const ff dprev = ff_add(L.prev, ff_of(I.mx.mpio2));
+                const bool cross = upd & (L.prev.hi > 0.f) & (ff_neg_sign(dprev) != ff_neg_sign(dt));
+                L.passes += cross ? 1 : 0;
+                L.prev.hi = upd ? L.x[2].hi : L.prev.hi;
+                L.prev.lo = upd ? L.x[2].lo : L.prev.lo;
             }
-            if (L.term == FOORT_TERMCODE_HORIZON) L.passes = -L.passes;
         }
         if (R.diag_flags & FOORT_DIAG_CLOSEST_RADIUS) {
             const bool d = (R.cr_every > 0) ? decide_nb(R.cr_every, L.cC)
@@ -840,11 +841,9 @@ struct MixedEngine {
         // A NaN or Inf anywhere in the state reaches r or u^r within one step through the
         // right-hand side, so those two words stand for the whole state here; the full
         // state is checked again when the geodesic's record is written.
-        if (!(isfinite(L.x[1].hi) && isfinite(L.v[1].hi))) {
-            L.err |= FOORT_ERR_NONFINITE;
-            if (L.term == FOORT_TERMCODE_CONTINUE && !(R.term_flags & FOORT_TERM_TIMEOUT)) return false;
-        }
-        return L.term == FOORT_TERMCODE_CONTINUE;
+        const bool bad = !(isfinite(L.x[1].hi) & isfinite(L.v[1].hi));
+        L.err |= bad ? FOORT_ERR_NONFINITE : 0u;
+        return (L.term == FOORT_TERMCODE_CONTINUE) & !(bad & !(R.term_flags & FOORT_TERM_TIMEOUT));
     }
 
     static __device__ __forceinline__ void write(const Lane& L, const RunConst& R, foort_result* o, int term,
@@ -854,7 +853,9 @@ struct MixedEngine {
         if (!(finite4(x) && finite4(v))) err |= FOORT_ERR_NONFINITE;
         DiagState D;
         D.quad = L.quad;
-        D.passes = L.passes;
+        if ((R.diag_flags & FOORT_DIAG_FOUR_COLOR_SCREEN) && term == FOORT_TERMCODE_BOUNDARY_SPHERE)
+            D.quad = four_color_quadrant(x[2], x[3]);
+        D.passes = ((R.diag_flags & FOORT_DIAG_EQUATORIAL_PASSES) && term == FOORT_TERMCODE_HORIZON) ? -L.passes : L.passes;
         double rm = -1.0;
         if (L.has_rmin) rm = R.rlog ? exp(ff_d(L.rmin)) : ff_d(L.rmin);
         if ((R.diag_flags & FOORT_DIAG_CLOSEST_RADIUS) && term == FOORT_TERMCODE_HORIZON) rm = 0.0;
