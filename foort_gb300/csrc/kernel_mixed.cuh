@@ -294,8 +294,10 @@ __device__ __noinline__ StepD step_fp64(const ImageConst& I, const RunConst& R, 
 // which is the reference's expression with eps factored out, with eps carried as a
 // float-float pair: the step size then has no systematic bias against the FP64 kernel's
 // (a bias would shift every ray's affine parameter, and strongly bent rays turn a shift
-// into an error of their end points). The quotient is formed from the reciprocal with its
-// residual: q0 = eps_hi (1/s), then q = q0 + (eps_hi - q0 s + eps_lo) / s. Taking eps_hi
+// into an error of their end points). h = eps / s is formed as eps m / d with
+// d = m (s1 + s3) + s2 (s = s1 + s2 / m + s3, m = min(theta, pi - theta)), so that one
+// reciprocal sits on the step's chain, and from that reciprocal with its residual:
+// q0 = eps_hi m (1/d), then q = q0 + (eps_hi m - q0 d + eps_lo m) / d. Taking eps_hi
 // times the rounded 1/s instead is biased: far from the hole s = |u^1| + ... lies just
 // below 1, where floats are twice as dense as just above 1, so every other 1/s falls just
 // past a rounding midpoint and rounds up, making h about 3e-8 too large on average; over
@@ -306,15 +308,18 @@ __device__ __forceinline__ float adaptive_step_f32(const RunConst& R, const Mixe
     // pi - theta to float accuracy: near theta = pi the high parts' difference is exact
     // (Sterbenz) and the low parts carry the rest
     const float t = ff_f(th), pt = __fadd_rn(__fsub_rn(mc.pi[0], th.hi), __fsub_rn(mc.pi[1], th.lo));
-    const float m = (pt < t) ? pt : t;
+    const float m = fabsf((pt < t) ? pt : t);
     const float s1 = __fadd_rn(fabsf(v[1]), 1e-20f);
-    const float s2 = __fmul_rn(__fadd_rn(fabsf(v[2]), 1e-20f), rcp(fabsf(m)));
+    const float s2 = __fadd_rn(fabsf(v[2]), 1e-20f);
     const float s3 = fabsf(__fadd_rn(v[3], 1e-20f));
-    const float sum = __fadd_rn(__fadd_rn(s1, s2), s3);
-    const float inv = rcp(sum);
-    const float q0 = __fmul_rn(mc.eps[0], inv);
-    const float res = __fmaf_rn(-q0, sum, mc.eps[0]);  // eps_hi - q0 s, exact
-    const float h = __fmaf_rn(__fadd_rn(res, mc.eps[1]), inv, q0);
+    // eps / (s1 + s2 / m + s3) = eps m / (m (s1 + s3) + s2): one reciprocal on the chain
+    // instead of two (1 / m, then 1 / s)
+    const float den = __fmaf_rn(m, __fadd_rn(s1, s3), s2);
+    const float inv = rcp(den);
+    const float num = __fmul_rn(mc.eps[0], m);
+    const float q0 = __fmul_rn(num, inv);
+    const float res = __fmaf_rn(-q0, den, num);  // num - q0 den, exact
+    const float h = __fmaf_rn(__fmaf_rn(mc.eps[1], m, res), inv, q0);
     const float hmin = mc.hmin;
     return (h < hmin) ? hmin : h;
 }
