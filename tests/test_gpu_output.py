@@ -144,3 +144,42 @@ def test_wave_schedule_under_a_pixel_budget_writes_the_round_files(engine_lib, t
     assert (s_r, s_w) == (abi.SCHEDULE_ROUNDS, abi.SCHEDULE_WAVES) and l_r == r_r
     if max_pixels == 100000:
         assert l_w < l_r
+
+
+def test_wave_schedule_over_two_images_writes_the_round_files(engine_lib, tmp_path):
+    """Two Kerr images in one run, each with its own V2 mesh (17^2 seed, MaxSubdivide 3,
+    IterationPixels 100), the first under a MaxPixels budget that cuts its rounds and the
+    second unlimited: the wave schedule (per-image waves, lookahead and budgets, one launch
+    per wave over both images) writes each image's files as the round-by-round schedule
+    does, byte for byte."""
+    import foort_gb300
+    wl = workloads.c2(abi.PREC_MIXED)
+    d = wl.desc
+    keep = abi.attach_images(d, [abi.make_image((0.99,), r=1000.0, theta=np.radians(60), half_width=12.0),
+                                 abi.make_image((0.7,), r=1000.0, theta=np.radians(35), half_width=10.0)])
+    specs = [("v2", dict(max_pixels=700, initial_pixels=17 * 17, max_subdivide=3, iteration_pixels=100)),
+             ("v2", dict(max_pixels=0, initial_pixels=17 * 17, max_subdivide=3, iteration_pixels=100))]
+    files, info = {}, {}
+    for schedule in (abi.SCHEDULE_ROUNDS, abi.SCHEDULE_WAVES):
+        meshes = [foort_gb300.Mesh.from_spec(sp, d.diag_flags, d.value_diag) for sp in specs]
+        outs = []
+        for i, m in enumerate(meshes):
+            od = tmp_path / f"s{schedule}_{i}"
+            od.mkdir()
+            outs.append(foort_gb300.Output(str(od / "run"), d.diag_flags, d.value_diag,
+                                           first_line=m.first_line_info(d, image=i)))
+        with foort_gb300.Engine(d) as e:
+            e.set_schedule(schedule)
+            info[schedule] = e.run(meshes, outs) + e.run_info()
+        for o in outs:
+            o.close()
+        for m in meshes:
+            m.close()
+        files[schedule] = {(i, f.name): f.read_bytes() for i in range(2)
+                           for f in sorted((tmp_path / f"s{schedule}_{i}").iterdir())}
+    del keep
+    assert files[abi.SCHEDULE_WAVES] == files[abi.SCHEDULE_ROUNDS] and len(files[abi.SCHEDULE_ROUNDS]) >= 4
+    g_r, r_r, l_r, s_r = info[abi.SCHEDULE_ROUNDS]
+    g_w, r_w, l_w, s_w = info[abi.SCHEDULE_WAVES]
+    assert (g_w, r_w) == (g_r, r_r) and (s_r, s_w) == (abi.SCHEDULE_ROUNDS, abi.SCHEDULE_WAVES)
+    assert l_w <= l_r == r_r  # the budgeted image's later rounds may each take a launch
