@@ -42,6 +42,13 @@
 //   5. with a finite MaxPixels, the queue is cut to the pixels left, in that order.
 // With FOORT_DMESH_ORDER_REFERENCE the rounds hand out the reference's pixels in the
 // reference's order.
+//
+// A whole run (foort_gpu_run_dmesh) launches by level waves where the mesh's MaxPixels is
+// unlimited: a device copy of the mesh with unlimited IterationPixels hands out one
+// subdivision level per round, each launch also takes the next level's candidates (the
+// five of every square awaiting its weight, deduplicated on the device) while it stays
+// within the context's lookahead cap, and every result is kept in a pool indexed by
+// slot[cell]. The mesh's own rounds then gather their results from the pool.
 #include <cuda_runtime.h>
 
 #include <cub/device/device_merge_sort.cuh>
