@@ -13,9 +13,12 @@
 // 66,000-71,000 steps, so a round of 1,079 geodesics takes as long as one of 16,384. With
 // unlimited MaxPixels the mesh's pixel set is fixed by the values alone
 // (foort_mesh_create_waves), and it splits into one wave per subdivision level, each
-// depending only on the results of the waves before. The run integrates the waves first
-// (C2: three launches where the reference has five rounds), then replays the meshes'
-// rounds from the stored results, so meshes and output files see the reference's rounds.
+// depending only on the results of the waves before. The run integrates the waves first,
+// a wave's launch also taking the next wave's candidates (foort_mesh_lookahead) while it
+// stays within the context's lookahead cap (C2: two launches where the reference has five
+// rounds), then replays the meshes' rounds from the stored results, so meshes and output
+// files see the reference's rounds. With a finite MaxPixels an image's waves stop at that
+// budget, and its rounds integrate what the waves did not.
 #include <algorithm>
 #include <cstring>
 #include <vector>
