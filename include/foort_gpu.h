@@ -614,8 +614,8 @@ int foort_gpu_run_info(const foort_ctx* ctx, uint32_t* launches, uint32_t* sched
  * then holds at most max_geodesics geodesics; the next wave then needs no launch of its
  * own. Candidates the run does not use are integrated and dropped: they reach neither
  * the meshes nor the files. 0 = off; FOORT_LOOKAHEAD_AUTO (default) = 128 x the GPU's SM
- * count (19,456 on GB300), about the geodesics a launch holds at two lanes each before
- * its warps share issue slots. */
+ * count (19,456 on GB300): at two lanes each, two warps per SM sub-partition, up to which
+ * a launch of such geodesics takes little longer than its longest geodesic alone. */
 #define FOORT_LOOKAHEAD_AUTO UINT64_MAX
 int foort_gpu_set_lookahead(foort_ctx* ctx, uint64_t max_geodesics);
 
