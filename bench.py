@@ -279,6 +279,7 @@ def run_sharded(args, rank, world, local):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     wl = workload(args.workload, abi.PREC_MIXED, args.iteration_pixels)
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
     with foort_gb300.Engine(wl.desc) as e:
         def one_run():
             n = [0, 0, 0]
@@ -290,8 +291,9 @@ def run_sharded(args, rank, world, local):
             def integrate(px):
                 n[2] += 1
                 return e.integrate(px)
+            # each rank's slice of a launch is held to foort_gpu_run's default lookahead cap
             multirank.sharded_run(wl.mesh, wl.desc, integrate, rank, world, dist, on_round=count,
-                                  waves=args.schedule == "waves")
+                                  waves=args.schedule == "waves", lookahead=128 * sms * world)
             return n
         for _ in range(args.warmup):
             n_geod, n_rounds, n_launch = one_run()

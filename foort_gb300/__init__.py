@@ -685,14 +685,36 @@ def _pixel_keys(px):
                                                  + px["col"].astype(np.int64))
 
 
-def run_by_waves(mesh_specs, desc, integrate, on_round=None):
-    """foort_gpu_run's level-wave schedule (without lookahead) with any integrate(px) ->
-    results: the meshes' level waves (Mesh.waves) are integrated first, one integrate()
-    call per wave, an image's waves stopping before the one that would take them past its
-    mesh's max_pixels; then the meshes' rounds are replayed from the stored results, so
-    on_round(px, res) sees the reference's rounds. A round's pixels that no wave held go
-    to integrate() then. Returns (rounds, integrate calls)."""
-    keys, results = [], []
+class _ResultStore:
+    """Results by pixel key (image, grid cell), kept sorted for lookups."""
+
+    def __init__(self):
+        self.k = np.zeros(0, np.int64)
+        self.r = np.zeros(0, abi.RESULT_DTYPE)
+
+    def add(self, px, res):
+        k = np.concatenate([self.k, _pixel_keys(px)])
+        r = np.concatenate([self.r, res])
+        order = np.argsort(k, kind="stable")
+        self.k, self.r = k[order], r[order]
+
+    def find(self, px):
+        q = _pixel_keys(px)
+        if not len(self.k):
+            return np.zeros(len(q), bool), np.zeros(len(q), abi.RESULT_DTYPE)
+        i = np.minimum(np.searchsorted(self.k, q), len(self.k) - 1)
+        return self.k[i] == q, self.r[i].copy()
+
+
+def run_by_waves(mesh_specs, desc, integrate, on_round=None, lookahead=0):
+    """foort_gpu_run's level-wave schedule with any integrate(px) -> results: the meshes'
+    level waves (Mesh.waves) are integrated first, one integrate() call per wave, an
+    image's waves stopping before the one that would take them past its mesh's
+    max_pixels; a call also takes the next wave's candidates (Mesh.lookahead) while it then
+    holds at most `lookahead` pixels (0: never). The meshes' rounds are then replayed from
+    the stored results, so on_round(px, res) sees the reference's rounds; a round's pixels
+    that no wave held go to integrate() then. Returns (rounds, integrate calls)."""
+    store = _ResultStore()
     meshes = [Mesh.from_spec(spec, desc.diag_flags, desc.value_diag) for spec in mesh_specs]
     waves = []
     for m in meshes:
@@ -712,31 +734,35 @@ def run_by_waves(mesh_specs, desc, integrate, on_round=None):
             if not live:
                 break
             parts = [w.pixels(image=i) for i, w in live]
-            px = np.concatenate(parts)
-            res = integrate(px)
-            calls += 1
-            keys.append(_pixel_keys(px))
-            results.append(res)
-            k = 0
             for (i, w), p in zip(live, parts):
                 w.handed += len(p)
+            px = np.concatenate(parts)
+            found, _ = store.find(px)
+            todo = px[~found]
+            if len(todo):
+                if lookahead > len(todo):
+                    cand = [w.lookahead(image=i) for i, w in live]
+                    if all(len(c) <= w.budget - w.handed for c, (i, w) in zip(cand, live)):
+                        cand = np.concatenate(cand)
+                        known, _ = store.find(cand)
+                        cand = cand[~known & ~np.isin(_pixel_keys(cand), _pixel_keys(todo))]
+                        if len(todo) + len(cand) <= lookahead:
+                            todo = np.concatenate([todo, cand])
+                store.add(todo, integrate(todo))
+                calls += 1
+            _, res = store.find(px)
+            k = 0
+            for (i, w), p in zip(live, parts):
                 w.set_results(res[k:k + len(p)])
                 w.end_round()
                 k += len(p)
     finally:
         for w in waves:
             w.close()
-    k = np.concatenate(keys) if keys else np.zeros(0, np.int64)
-    r = np.concatenate(results) if results else np.zeros(0, abi.RESULT_DTYPE)
-    order = np.argsort(k, kind="stable")
-    k, r = k[order], r[order]
     extra = [0]
 
     def lookup(px):
-        q = _pixel_keys(px)
-        i = np.minimum(np.searchsorted(k, q), max(len(k) - 1, 0))
-        found = (k[i] == q) if len(k) else np.zeros(len(q), bool)
-        res = r[i].copy() if len(k) else np.zeros(len(q), abi.RESULT_DTYPE)
+        found, res = store.find(px)
         if not found.all():
             res[~found] = integrate(px[~found])
             extra[0] += 1

@@ -61,7 +61,7 @@ def sharded_round(px, integrate, rank, world, dist=None):
     return out
 
 
-def sharded_run(mesh_specs, desc, integrate, rank, world, dist=None, on_round=None, waves=False):
+def sharded_run(mesh_specs, desc, integrate, rank, world, dist=None, on_round=None, waves=False, lookahead=0):
     """One FOORT run (Main.cpp:313-419) sharded over `world` ranks. Every rank holds an
     identical copy of the meshes, so every rank computes the same pixel list for a round;
     each rank integrates its contiguous slice with integrate(slice) -> results, the slices
@@ -69,11 +69,12 @@ def sharded_run(mesh_specs, desc, integrate, rank, world, dist=None, on_round=No
     meshes (Mesh::GeodesicFinished, Main.cpp:399) before they end the round
     (Mesh::EndCurrentLoop, Main.cpp:410). The gather is the run's only exchange, once per
     round. waves: the meshes' level waves are sharded and gathered instead (one exchange
-    per wave) and the rounds replayed from their results (foort_gb300.run_by_waves).
+    per wave) and the rounds replayed from their results (foort_gb300.run_by_waves, with
+    `lookahead` the most pixels one sharded launch may hold, over all ranks).
     Returns the number of rounds; on_round(px, res) sees each whole round."""
     from . import run_by_waves, run_rounds
     shard = lambda px: sharded_round(px, integrate, rank, world, dist)  # noqa: E731
     if waves:
-        return run_by_waves(mesh_specs, desc, shard, on_round)[0]
+        return run_by_waves(mesh_specs, desc, shard, on_round, lookahead=lookahead)[0]
     return run_rounds(mesh_specs, desc, shard, on_round)
 

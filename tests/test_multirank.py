@@ -139,19 +139,21 @@ def test_sharded_c2_shaped_run_hands_out_the_single_rank_pixels(oracle_mod, tmp_
     del keep
 
 
+@pytest.mark.parametrize("lookahead", [0, 100000])
 @pytest.mark.parametrize("max_pixels", [0, 150])
-def test_run_by_waves_matches_the_round_loop(oracle_mod, max_pixels):
+def test_run_by_waves_matches_the_round_loop(oracle_mod, max_pixels, lookahead):
     """foort_gb300.run_by_waves (the level-wave schedule with any integrator, here the
     oracle) hands out the round loop's pixels and results, round by round, with or without
-    a MaxPixels budget that cuts the rounds; with the budget its waves stop and the rounds
-    integrate the rest."""
+    a MaxPixels budget that cuts the rounds and with or without lookahead; with the budget
+    its waves stop and the rounds integrate the rest."""
     import foort_gb300
     d, mesh, keep = _c2_shaped()
     spec = [(mesh[0][0], dict(mesh[0][1], max_pixels=max_pixels))]
     integ = lambda p: oracle_mod.integrate(d, p, fast=False)  # noqa: E731
     a, b = [], []
     ra = foort_gb300.run_rounds(spec, d, integ, on_round=lambda px, res: a.append((px.copy(), res.copy())))
-    rb, calls = foort_gb300.run_by_waves(spec, d, integ, on_round=lambda px, res: b.append((px.copy(), res.copy())))
+    rb, calls = foort_gb300.run_by_waves(spec, d, integ, on_round=lambda px, res: b.append((px.copy(), res.copy())),
+                                         lookahead=lookahead)
     assert ra == rb == len(a) == len(b) >= 2
     for (pa, xa), (pb, xb) in zip(a, b):
         assert np.array_equal(pa, pb)
@@ -161,4 +163,6 @@ def test_run_by_waves_matches_the_round_loop(oracle_mod, max_pixels):
         assert sum(len(p) for p, _ in a) <= max_pixels
     else:
         assert calls < ra
+        if lookahead:  # MaxSubdivide 3: the seed, then one launch for both finer levels
+            assert calls == 2
     del keep
