@@ -418,6 +418,10 @@ class Mesh:
         """Most pixels the mesh hands out over a run (0: no limit)."""
         return self._lib.foort_mesh_max_pixels(self._m)
 
+    def kind(self):
+        """abi.MESH_SIMPLE or abi.MESH_SUBDIVISION_V2."""
+        return self._lib.foort_mesh_kind(self._m)
+
     def lookahead(self, image=0):
         """foort_mesh_lookahead: candidates of the next round of a mesh of level waves."""
         n = C.c_uint64()

@@ -31,6 +31,10 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_FP64_ANALYTIC = 2  # every step in FP64 with the mixed kernel's analytic derivatives
 
+# mesh kinds (foort_mesh_kind)
+MESH_SIMPLE = 0
+MESH_SUBDIVISION_V2 = 1
+
 # foort_gpu_run's schedule (include/foort_gpu.h)
 SCHEDULE_WAVES = 0
 SCHEDULE_ROUNDS = 1

@@ -179,3 +179,20 @@ def test_lookahead_holds_the_next_wave(engine_lib, case):
         assert len(cand) == len(la) and np.all(la["grid"] == grid)
         waves.set_values([oracle.synth_value(vk, a, b, grid) for a, b in zip(px["row"], px["col"])])
         waves.end_round()
+
+
+def test_mesh_kind_and_pixel_cap(engine_lib):
+    """foort_mesh_kind and foort_mesh_max_pixels; a SimpleSquareMesh is its own single wave
+    with no lookahead candidates."""
+    import foort_gb300
+    simple = foort_gb300.Mesh("simple", abi.DIAG_FOUR_COLOR_SCREEN, abi.DIAG_FOUR_COLOR_SCREEN, total_pixels=40 * 40)
+    v2 = foort_gb300.Mesh("v2", abi.DIAG_FOUR_COLOR_SCREEN, abi.DIAG_FOUR_COLOR_SCREEN, max_pixels=500,
+                          initial_pixels=81, max_subdivide=3, iteration_pixels=10)
+    assert (simple.kind(), v2.kind()) == (abi.MESH_SIMPLE, abi.MESH_SUBDIVISION_V2)
+    assert (simple.max_pixels(), v2.max_pixels()) == (1600, 500)
+    assert engine_lib.foort_mesh_kind(None) == abi.FOORT_E_BADARG
+    w = simple.waves()
+    assert w.kind() == abi.MESH_SIMPLE and w.size() == 1600 and len(w.lookahead()) == 0
+    w.set_values([0.0] * 1600)
+    w.end_round()
+    assert w.finished()
