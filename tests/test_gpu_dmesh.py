@@ -207,3 +207,47 @@ def test_run_dmesh_rejects_a_small_result_buffer(eng):
         with pytest.raises(eng.FoortError) as ei:
             dmesh.run(e, out.data_ptr(), 80)
         assert ei.value.code == abi.FOORT_E_BADARG and "80" in str(ei.value)
+
+
+@pytest.mark.parametrize("value_diag,max_pixels", [(abi.DIAG_EQUATORIAL_PASSES, 0), (abi.DIAG_CLOSEST_RADIUS, 0),
+                                                   (abi.DIAG_FOUR_COLOR_SCREEN, 1500)])
+def test_run_dmesh_other_values_and_a_pixel_budget(eng, value_diag, max_pixels):
+    """foort_gpu_run_dmesh with EquatorialPasses or ClosestRadius as the mesh's value (the
+    device scatters the value the reference's vector starts with) and with a finite
+    MaxPixels (the device mesh then goes round by round, cutting the last round as the
+    reference does): the host loop's pixels and results, bit for bit."""
+    import torch
+    wl = workloads.c2(abi.PREC_MIXED)
+    d = wl.desc
+    d.diag_flags = abi.DIAG_FOUR_COLOR_SCREEN | abi.DIAG_EQUATORIAL_PASSES | abi.DIAG_CLOSEST_RADIUS
+    d.value_diag = value_diag
+    spec = dict(max_pixels=max_pixels, initial_pixels=25 * 25, max_subdivide=3, iteration_pixels=120,
+                initial_sub_to_final=0)
+    host_rounds = []
+    with eng.Engine(d) as e:
+        mesh = eng.Mesh("v2", d.diag_flags, d.value_diag, **spec)
+        while not mesh.finished():
+            px = mesh.pixels()
+            res = e.integrate(px)
+            host_rounds.append((px, res))
+            mesh.set_results(res)
+            mesh.end_round()
+        dev_rounds = []
+        dmesh = eng.DeviceMesh(d.diag_flags, d.value_diag, **spec)
+        cap = 5 * 120 + 25 * 25
+        out = torch.zeros(cap * abi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+
+        def on_round(d_px, d_res, n, rnd):
+            dev_rounds.append((dmesh.pixels(), np.frombuffer(out[:n * abi.RESULT_DTYPE.itemsize].cpu().numpy().tobytes(),
+                                                             dtype=abi.RESULT_DTYPE)))
+
+        g, r = dmesh.run(e, out.data_ptr(), cap, on_round)
+        _, used = e.run_info()
+    assert r == len(host_rounds) == len(dev_rounds) >= 2
+    assert used == (abi.SCHEDULE_ROUNDS if max_pixels else abi.SCHEDULE_WAVES)
+    if max_pixels:
+        assert g <= max_pixels
+    for k, ((hp, hr), (dp, dr)) in enumerate(zip(host_rounds, dev_rounds)):
+        assert np.array_equal(hp, dp), k
+        for name in abi.RESULT_DTYPE.names:
+            np.testing.assert_array_equal(hr[name], dr[name], err_msg=f"round {k}: {name}")
