@@ -134,23 +134,41 @@ int launch(foort_ctx* ctx, const std::vector<foort_pixel>& px, std::vector<foort
 }
 
 // The next wave's candidates (foort_mesh_lookahead) of the images marked in `use` that have
-// no result yet and are not in `todo`, appended to `spec`.
+// no result yet and are not in `todo`, appended to `spec`. Stops, with `over` set, once
+// there are more than `limit` of them: the launch then cannot take them.
 int lookahead_candidates(foort_mesh* const* waves, uint32_t n_images, const std::vector<bool>& use,
-                         const ResultStore& store, const std::vector<foort_pixel>& todo,
-                         std::vector<foort_pixel>& spec) {
+                         const ResultStore& store, const std::vector<foort_pixel>& todo, uint64_t limit,
+                         std::vector<foort_pixel>& spec, bool& over) {
+    over = false;
+    std::vector<uint64_t> raw(n_images, 0);
+    uint64_t known = store.res.size() + todo.size();  // candidates that can drop out, at most
+    uint64_t all = 0;
+    for (uint32_t i = 0; i < n_images; ++i) {
+        if (!use[i]) continue;
+        const int rc = foort_mesh_lookahead(waves[i], i, nullptr, 0, &raw[i]);
+        if (rc) return rc;
+        all += raw[i];
+    }
+    if (all > limit + known) {  // more than `limit` remain whatever drops out
+        over = true;
+        return FOORT_OK;
+    }
     PixelMap now;
     for (const foort_pixel& p : todo) now.put(PixelMap::key(p), 0);
     std::vector<foort_pixel> cand;
     for (uint32_t i = 0; i < n_images; ++i) {
-        if (!use[i]) continue;
-        uint64_t n = 0;
-        int rc = foort_mesh_lookahead(waves[i], i, nullptr, 0, &n);
-        if (rc) return rc;
+        if (!use[i] || raw[i] == 0) continue;
+        uint64_t n = raw[i];
         cand.resize(n);
-        if (n && (rc = foort_mesh_lookahead(waves[i], i, cand.data(), n, &n))) return rc;
+        const int rc = foort_mesh_lookahead(waves[i], i, cand.data(), n, &n);
+        if (rc) return rc;
         for (const foort_pixel& p : cand) {
             const uint64_t k = PixelMap::key(p);
             if (!store.slot.has(k) && !now.has(k)) spec.push_back(p);
+        }
+        if (spec.size() > limit) {
+            over = true;
+            return FOORT_OK;
         }
     }
     return FOORT_OK;
@@ -205,12 +223,15 @@ int integrate_waves(foort_ctx* ctx, foort_mesh* const* meshes, uint32_t n_images
         if (!todo.empty()) {
             if (ahead > todo.size()) {
                 std::vector<foort_pixel> spec;
+                bool over = false;
                 for (uint32_t i = 0; i < n_images; ++i) use[i] = count[i] > 0;
-                if ((rc = lookahead_candidates(waves.data(), n_images, use, store, todo, spec))) break;
+                if ((rc = lookahead_candidates(waves.data(), n_images, use, store, todo, ahead - todo.size(), spec,
+                                               over)))
+                    break;
                 // candidates within each image's budget only
                 std::vector<uint64_t> per(n_images, 0);
                 for (const foort_pixel& p : spec) ++per[p.image];
-                bool fits = todo.size() + spec.size() <= ahead;
+                bool fits = !over && todo.size() + spec.size() <= ahead;
                 for (uint32_t i = 0; i < n_images && fits; ++i) fits = per[i] <= budget[i] - handed[i];
                 if (fits) todo.insert(todo.end(), spec.begin(), spec.end());
             }

@@ -196,3 +196,31 @@ def test_mesh_kind_and_pixel_cap(engine_lib):
     w.set_values([0.0] * 1600)
     w.end_round()
     assert w.finished()
+
+
+@pytest.mark.parametrize("init,maxsub,vk", [(9, 9, 0), (25, 6, 2), (129 * 129, 2, 0)])
+def test_lookahead_ascending_on_sparse_and_dense_grids(engine_lib, init, maxsub, vk):
+    """The candidates come out in ascending cell order, each once, whether the grid is much
+    larger than the candidate list (a 3 x 3 seed on a 513-cell side: the early rounds sort the
+    list) or not (the later rounds, the 129 x 129 seed: a bitmap of the grid), and every round's candidates hold the next round's pixels."""
+    import foort_gb300
+    mesh = foort_gb300.Mesh("v2", abi.DIAG_FOUR_COLOR_SCREEN, abi.DIAG_FOUR_COLOR_SCREEN, max_pixels=0,
+                            initial_pixels=init, max_subdivide=maxsub, iteration_pixels=1000, initial_sub_to_final=0)
+    grid = mesh.grid()
+    waves = mesh.waves()
+    mesh.close()
+    cand, sizes, rounds = None, [], 0
+    while not waves.finished() and rounds < 6:
+        px = waves.pixels()
+        cells = px["row"].astype(np.int64) * grid + px["col"].astype(np.int64)
+        if cand is not None:
+            assert np.isin(cells, cand).all()
+        la = waves.lookahead()
+        cand = la["row"].astype(np.int64) * grid + la["col"].astype(np.int64)
+        assert np.all(np.diff(cand) > 0)
+        sizes.append(len(cand))
+        waves.set_values([oracle.synth_value(vk, a, b, grid) for a, b in zip(px["row"], px["col"])])
+        waves.end_round()
+        rounds += 1
+    waves.close()
+    assert rounds >= 2 and max(sizes) > 0
