@@ -201,8 +201,9 @@ def test_mesh_kind_and_pixel_cap(engine_lib):
 @pytest.mark.parametrize("init,maxsub,vk", [(9, 9, 0), (25, 6, 2), (129 * 129, 2, 0)])
 def test_lookahead_ascending_on_sparse_and_dense_grids(engine_lib, init, maxsub, vk):
     """The candidates come out in ascending cell order, each once, whether the grid is much
-    larger than the candidate list (a 3 x 3 seed on a 513-cell side: the early rounds sort the
-    list) or not (the later rounds, the 129 x 129 seed: a bitmap of the grid), and every round's candidates hold the next round's pixels."""
+    larger than the candidate list (a 3 x 3 seed on a 513-cell side: the early rounds sort
+    the list) or not (the later rounds, the 129 x 129 seed: a bitmap of the grid), and every
+    round's candidates hold the next round's pixels."""
     import foort_gb300
     mesh = foort_gb300.Mesh("v2", abi.DIAG_FOUR_COLOR_SCREEN, abi.DIAG_FOUR_COLOR_SCREEN, max_pixels=0,
                             initial_pixels=init, max_subdivide=maxsub, iteration_pixels=1000, initial_sub_to_final=0)
