@@ -11,7 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <memory>
+#include <deque>
 #include <string>
 #include <vector>
 
@@ -29,17 +29,29 @@ uint32_t first_diagnostic(uint32_t diag_flags, uint32_t value_diag) {
     return order.empty() ? 0u : order[0];
 }
 
+// A pixel's value vector as the distances read it: its length and its first two entries
+// (no distance reads further).
+struct Value {
+    double v[2] = {0.0, 0.0};
+    uint32_t n = 0;
+    void set(const double* x, uint32_t len) {
+        n = len;
+        for (uint32_t i = 0; i < len && i < 2; ++i) v[i] = x[i];
+    }
+};
+
 // FinalDataValDistance of the value diagnostic (Diagnostics.cpp:214-221, :311-322,
 // :395-401, :460-464).
-double distance(uint32_t value_diag, const std::vector<double>& a, const std::vector<double>& b) {
-    if (a.empty() || b.empty()) return 0.0;
+double distance(uint32_t value_diag, const Value& a, const Value& b) {
+    if (a.n == 0 || b.n == 0) return 0.0;
     switch (value_diag) {
-    case FOORT_DIAG_FOUR_COLOR_SCREEN: return std::fabs(a[0] - b[0]) < 1.0 ? 0.0 : 1.0;
+    case FOORT_DIAG_FOUR_COLOR_SCREEN: return std::fabs(a.v[0] - b.v[0]) < 1.0 ? 0.0 : 1.0;
     case FOORT_DIAG_GEODESIC_POSITION:
-        if (a.size() != 2 || b.size() != 2) return 0.0;
-        return std::acos(std::cos(a[0]) * std::cos(b[0]) + std::sin(a[0]) * std::sin(b[0]) * std::cos(a[1] - b[1]));
-    case FOORT_DIAG_EQUATORIAL_PASSES: return std::fabs(a[0] - b[0]);  // pass counts are integers
-    default: return std::fabs(a[0] - b[0]);
+        if (a.n != 2 || b.n != 2) return 0.0;
+        return std::acos(std::cos(a.v[0]) * std::cos(b.v[0]) +
+                         std::sin(a.v[0]) * std::sin(b.v[0]) * std::cos(a.v[1] - b.v[1]));
+    case FOORT_DIAG_EQUATORIAL_PASSES: return std::fabs(a.v[0] - b.v[0]);  // pass counts are integers
+    default: return std::fabs(a.v[0] - b.v[0]);
     }
 }
 
@@ -59,7 +71,7 @@ struct foort_mesh {
     virtual ~foort_mesh() = default;
     virtual uint64_t cur() const = 0;
     virtual void pixel(uint64_t i, uint64_t& row, uint64_t& col) const = 0;
-    virtual void finished(uint64_t i, std::vector<double> v) = 0;
+    virtual void finished(uint64_t i, const double* v, uint32_t n) = 0;
     virtual void end_loop() = 0;
     virtual bool done() const = 0;
     virtual uint64_t rounds() const = 0;
@@ -85,7 +97,7 @@ struct SimpleMesh final : foort_mesh {
         row = i / grid;  // the reference counts rows up one by one (Mesh.cpp:40-43)
         col = i - row * grid;
     }
-    void finished(uint64_t, std::vector<double>) override {}
+    void finished(uint64_t, const double*, uint32_t) override {}
     void end_loop() override { fin = true; }
     bool done() const override { return fin; }
     uint64_t rounds() const override { return fin ? 1 : 0; }
@@ -108,7 +120,7 @@ struct V2Mesh final : foort_mesh {
         uint64_t row, col;
         int level;
         double weight = -1;
-        std::vector<double> value;
+        Value value;
         Px *left = nullptr, *right = nullptr, *up = nullptr, *down = nullptr, *se = nullptr;
         Px(uint64_t r, uint64_t c, int l) : row(r), col(c), level(l) {}
     };
@@ -116,12 +128,13 @@ struct V2Mesh final : foort_mesh {
     int max_sub = 1;
     bool infinite = true, sub_to_final = false;
     uint64_t n_rounds = 0;
-    std::vector<std::unique_ptr<Px>> all;  // owns every pixel (stable addresses)
+    bool waves = false;                    // a copy of level waves (wave_clone)
+    std::deque<Px> all;                    // owns every pixel (stable addresses, few allocations)
     std::vector<Px*> active, queue, updating;
 
     Px* make(uint64_t r, uint64_t c, int l) {
-        all.emplace_back(new Px(r, c, l));
-        return all.back().get();
+        all.emplace_back(r, c, l);
+        return &all.back();
     }
 
     // InitializeFirstGrid, Mesh.cpp:741-802
@@ -235,7 +248,7 @@ struct V2Mesh final : foort_mesh {
         row = queue[i]->row;
         col = queue[i]->col;
     }
-    void finished(uint64_t i, std::vector<double> v) override { queue[i]->value = std::move(v); }
+    void finished(uint64_t i, const double* v, uint32_t n) override { queue[i]->value.set(v, n); }
     bool done() const override { return queue.empty(); }
     uint64_t rounds() const override { return n_rounds; }
     // Mesh.cpp:697-707
@@ -266,6 +279,7 @@ struct V2Mesh final : foort_mesh {
         m->max_sub = max_sub;
         m->iteration = UINT64_MAX;
         m->sub_to_final = sub_to_final;
+        m->waves = true;
         m->init_grid();
         return m;
     }
@@ -299,6 +313,28 @@ struct V2Mesh final : foort_mesh {
         cells.erase(std::unique(cells.begin(), cells.end()), cells.end());
     }
 
+    // The reference's std::sort of the active list (Mesh.cpp:1126-1130), on records that
+    // carry each square's weight and level beside its pointer: std::sort's permutation
+    // depends only on the element count and the comparisons' outcomes, which are the same
+    // as on the pointers, so the order (ties included) is the reference's, without a
+    // pointer dereference per comparison.
+    struct SortKey {
+        double weight;
+        int level;
+        Px* p;
+    };
+    std::vector<SortKey> keys;
+    void sort_active() {
+        keys.resize(active.size());
+        for (size_t i = 0; i < active.size(); ++i) keys[i] = SortKey{active[i]->weight, active[i]->level, active[i]};
+        std::sort(keys.begin(), keys.end(), [](const SortKey& a, const SortKey& b) {
+            if (a.weight > b.weight) return true;
+            if (a.weight == b.weight && a.level < b.level) return true;
+            return false;
+        });
+        for (size_t i = 0; i < active.size(); ++i) active[i] = keys[i].p;
+    }
+
     // EndCurrentLoop, Mesh.cpp:1092-1186
     void end_loop() override {
         ++n_rounds;
@@ -306,11 +342,11 @@ struct V2Mesh final : foort_mesh {
         queue.clear();
         if (infinite || left_px > 0) {
             update_weights();
-            std::sort(active.begin(), active.end(), [](const Px* a, const Px* b) {
-                if (a->weight > b->weight) return true;
-                if (a->weight == b->weight && a->level < b->level) return true;
-                return false;
-            });
+            // A wave copy subdivides every square of positive weight: the pixels it
+            // creates, their levels and links do not depend on the order (a shared
+            // pixel is made by one square and found by the other), only the order in
+            // which they are handed out does, and no result depends on that.
+            if (!waves) sort_active();
             const uint64_t lim = std::min<uint64_t>(active.size(), iteration);
             for (uint64_t i = 0; i < lim; ++i) subdivide(i);
             active.erase(active.begin(), active.begin() + static_cast<std::ptrdiff_t>(lim));
@@ -385,7 +421,7 @@ int foort_mesh_get_pixels(const foort_mesh* m, uint32_t image, foort_pixel* out)
 
 int foort_mesh_geodesic_finished(foort_mesh* m, uint64_t index, const double* values, uint32_t n_values) {
     if (!m || index >= m->cur() || (n_values && !values)) return FOORT_E_BADARG;
-    m->finished(index, std::vector<double>(values, values + n_values));
+    m->finished(index, values, n_values);
     return FOORT_OK;
 }
 
@@ -398,7 +434,7 @@ int foort_mesh_set_results(foort_mesh* m, const foort_result* res, uint64_t n) {
         if (first == FOORT_DIAG_FOUR_COLOR_SCREEN) v = res[i].quadrant;
         else if (first == FOORT_DIAG_EQUATORIAL_PASSES) v = res[i].equat_passes;
         else if (first == FOORT_DIAG_CLOSEST_RADIUS) v = res[i].closest_r;
-        m->finished(i, std::vector<double>{v});
+        m->finished(i, &v, 1);
     }
     return FOORT_OK;
 }
