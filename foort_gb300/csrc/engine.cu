@@ -25,7 +25,11 @@ struct foort_ctx {
     std::vector<ImageConst> hic;
     ImageConst* d_images = nullptr;
     unsigned long long* d_ctr = nullptr;
-    unsigned long long h_ctr[kNumCtr] = {};
+    // Pinned, so that the copy of the counters after a launch does not hold the host until
+    // the kernel ends (a copy into pageable memory returns only once it is done).
+    unsigned long long* h_ctr = nullptr;
+    foort_result* h_stage = nullptr;  // pinned results of a run's launch in flight
+    uint64_t stage_cap = 0;
     int32_t* h_cancel = nullptr;
     int32_t* d_cancel = nullptr;
     cudaStream_t stream = nullptr;
@@ -535,6 +539,9 @@ int foort_gpu_create(const foort_run_desc* desc, foort_ctx** out_ctx) {
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaMemcpy(images)"));
     e = cudaMalloc(&ctx->d_ctr, kNumCtr * sizeof(unsigned long long));
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaMalloc(counters)"));
+    e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_ctr), kNumCtr * sizeof(unsigned long long), cudaHostAllocDefault);
+    if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaHostAlloc(counters)"));
+    std::memset(ctx->h_ctr, 0, kNumCtr * sizeof(unsigned long long));
     e = cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_cancel), sizeof(int32_t), cudaHostAllocMapped);
     if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaHostAlloc(cancel)"));
     *ctx->h_cancel = 0;
@@ -747,6 +754,38 @@ void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule
     ctx->run_launches = launches;
     ctx->run_schedule = schedule;
 }
+// foort_gpu_integrate in two halves, for foort_gpu_run to work on the host while a launch
+// runs: begin enqueues the copy of n pixels from host memory, the launch and the copy of
+// the results into pinned memory, and returns; end waits for them and copies the results
+// out. Nothing else may launch on the context in between.
+int foort_ctx_integrate_begin(foort_ctx* ctx, const foort_pixel* px, uint64_t n) {
+    if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
+    if (n && !px) return fail(ctx, FOORT_E_BADARG, "NULL pixel buffer");
+    for (uint64_t i = 0; i < n; ++i)
+        if (px[i].image >= ctx->hic.size() || px[i].grid < 2)
+            return fail(ctx, FOORT_E_BADARG, "pixel " + std::to_string(i) + " has an invalid image index or grid < 2");
+    int rc = finish(ctx);
+    if (rc != FOORT_OK && rc != FOORT_E_BUDGET && rc != FOORT_E_CANCELLED) return rc;
+    if ((rc = ensure_capacity(ctx, n))) return rc;
+    if (n > ctx->stage_cap) {
+        if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+        ctx->h_stage = nullptr;
+        ctx->stage_cap = 0;
+        CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_stage), n * sizeof(foort_result), cudaHostAllocDefault));
+        ctx->stage_cap = n;
+    }
+    cudaStream_t st = ctx->stream;
+    if (n) CK(cudaMemcpyAsync(ctx->d_px, px, n * sizeof(foort_pixel), cudaMemcpyHostToDevice, st));
+    if ((rc = launch(ctx, ctx->d_px, n, ctx->d_out, st))) return rc;
+    if (n) CK(cudaMemcpyAsync(ctx->h_stage, ctx->d_out, n * sizeof(foort_result), cudaMemcpyDeviceToHost, st));
+    return FOORT_OK;
+}
+int foort_ctx_integrate_end(foort_ctx* ctx, foort_result* out, uint64_t n) {
+    const int rc = finish(ctx);
+    if (n && (rc == FOORT_OK || rc == FOORT_E_BUDGET || rc == FOORT_E_CANCELLED))
+        std::memcpy(out, ctx->h_stage, n * sizeof(foort_result));
+    return rc;
+}
 
 int foort_gpu_get_desc(const foort_ctx* ctx, foort_run_desc* desc) {
     if (!ctx || !desc) return FOORT_E_BADARG;
@@ -768,6 +807,8 @@ void foort_gpu_destroy(foort_ctx* ctx) {
     if (ctx->d_images) cudaFree(ctx->d_images);
     if (ctx->d_ctr) cudaFree(ctx->d_ctr);
     if (ctx->h_cancel) cudaFreeHost(ctx->h_cancel);
+    if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

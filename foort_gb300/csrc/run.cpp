@@ -18,7 +18,8 @@
 // stays within the context's lookahead cap (C2: two launches where the reference has five
 // rounds), then replays the meshes' rounds from the stored results, so meshes and output
 // files see the reference's rounds. With a finite MaxPixels an image's waves stop at that
-// budget, and its rounds integrate what the waves did not.
+// budget, and its rounds integrate what the waves did not. While a wave's launch runs, the
+// host replays the rounds whose results are already stored.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -33,6 +34,8 @@ uint64_t foort_ctx_budget(const foort_ctx* ctx);
 uint64_t foort_ctx_lookahead(const foort_ctx* ctx);
 void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule);
 void foort_ctx_launched(foort_ctx* ctx, const foort_pixel* px, uint64_t n, bool first);
+int foort_ctx_integrate_begin(foort_ctx* ctx, const foort_pixel* px, uint64_t n);
+int foort_ctx_integrate_end(foort_ctx* ctx, foort_result* out, uint64_t n);
 }
 
 namespace {
@@ -133,6 +136,20 @@ int launch(foort_ctx* ctx, const std::vector<foort_pixel>& px, std::vector<foort
     return foort_gpu_integrate(ctx, px.data(), px.size(), res.data());
 }
 
+// The same launch in two halves: `during` runs on the host while it is in flight.
+template <typename F>
+int launch_overlapped(foort_ctx* ctx, const std::vector<foort_pixel>& px, std::vector<foort_result>& res,
+                      uint32_t& launches, F&& during) {
+    res.resize(px.size());
+    foort_ctx_launched(ctx, px.data(), px.size(), launches == 0);
+    ++launches;
+    int rc = foort_ctx_integrate_begin(ctx, px.data(), px.size());
+    if (rc) return rc;
+    const int rc_host = during();
+    rc = foort_ctx_integrate_end(ctx, res.data(), px.size());
+    return rc ? rc : rc_host;
+}
+
 // The next wave's candidates (foort_mesh_lookahead) of the images marked in `use` that have
 // no result yet and are not in `todo`, appended to `spec`. Stops, with `over` set, once
 // there are more than `limit` of them: the launch then cannot take them.
@@ -178,8 +195,9 @@ int lookahead_candidates(foort_mesh* const* waves, uint32_t n_images, const std:
 // result. An image's waves stop before the one that would take them past the mesh's
 // foort_mesh_max_pixels (its rounds then find the rest missing and integrate it).
 // FOORT_E_UNSUPPORTED (nothing integrated) where a mesh has no waves.
+template <typename F>
 int integrate_waves(foort_ctx* ctx, foort_mesh* const* meshes, uint32_t n_images, ResultStore& store,
-                    uint32_t& launches) {
+                    uint32_t& launches, F&& during) {
     std::vector<foort_mesh*> waves(n_images, nullptr);
     auto release = [&]() {
         for (foort_mesh* w : waves) foort_mesh_destroy(w);
@@ -235,7 +253,7 @@ int integrate_waves(foort_ctx* ctx, foort_mesh* const* meshes, uint32_t n_images
                 for (uint32_t i = 0; i < n_images && fits; ++i) fits = per[i] <= budget[i] - handed[i];
                 if (fits) todo.insert(todo.end(), spec.begin(), spec.end());
             }
-            if ((rc = launch(ctx, todo, got, launches))) break;
+            if ((rc = launch_overlapped(ctx, todo, got, launches, during))) break;
             for (uint64_t g = 0; g < todo.size(); ++g) {
                 store.slot.put(PixelMap::key(todo[g]), store.res.size());
                 store.res.push_back(got[g]);
@@ -282,41 +300,46 @@ int results_from_store(foort_ctx* ctx, const ResultStore& store, const std::vect
     return FOORT_OK;
 }
 
-int run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs, uint32_t n_images,
-        uint64_t* geodesics, uint32_t* rounds, uint32_t& launches, uint32_t& schedule) {
-    foort_run_desc desc;
-    if (foort_gpu_get_desc(ctx, &desc)) return FOORT_E_BADARG;
-    const bool geopos = (desc.diag_flags & FOORT_DIAG_GEODESIC_POSITION) != 0;
-    const std::vector<uint32_t> order = foort::diagnostic_order(desc.diag_flags, desc.value_diag);
-    const uint32_t value_first = order.empty() ? 0u : order[0];
-    int rc = FOORT_OK;
-    ResultStore store;
-    schedule = FOORT_SCHEDULE_ROUNDS;
-    // A SimpleSquareMesh is its own single wave: without an adaptive mesh the waves are
-    // the rounds, and storing the results would only cost time.
-    bool adaptive = false;
-    for (uint32_t i = 0; i < n_images; ++i) adaptive = adaptive || foort_mesh_kind(meshes[i]) == FOORT_MESH_SUBDIVISION_V2;
-    if (adaptive && foort_ctx_schedule(ctx) == FOORT_SCHEDULE_WAVES && !geopos && foort_ctx_budget(ctx) == 0) {
-        rc = integrate_waves(ctx, meshes, n_images, store, launches);
-        if (rc == FOORT_OK) {
-            schedule = FOORT_SCHEDULE_WAVES;
-        } else if (rc != FOORT_E_UNSUPPORTED) {
-            return rc;
-        }
-    }
+// The reference's round loop (Main.cpp:313-419), one round per call of next().
+struct Rounds {
+    foort_ctx* ctx;
+    foort_mesh* const* meshes;
+    foort_output* const* outputs;
+    uint32_t n_images;
+    bool geopos;
+    uint32_t value_first;
     uint64_t total = 0;
     uint32_t n_rounds = 0;
+    bool done = false;
     std::vector<foort_pixel> px;
     std::vector<foort_result> res;
-    std::vector<uint64_t> count(n_images);
-    for (;;) {
+    std::vector<uint64_t> count;
+
+    // One round over every unfinished mesh. Its results come from `store` where given
+    // (with one launch for the pixels it lacks), else from a launch. stored_only: run the
+    // round only if the store holds all of its results (ran tells), and never launch.
+    int next(const ResultStore* store, uint32_t& launches, bool stored_only, bool& ran) {
+        ran = false;
+        if (done) return FOORT_OK;
         bool any = false;
-        if ((rc = gather(meshes, n_images, px, count, any))) return rc;
-        if (!any) break;
+        count.resize(n_images);
+        int rc = gather(meshes, n_images, px, count, any);
+        if (rc) return rc;
+        if (!any) {
+            done = true;
+            return FOORT_OK;
+        }
         const uint64_t n = px.size();
         res.resize(n);
-        if (schedule == FOORT_SCHEDULE_WAVES) {
-            rc = results_from_store(ctx, store, px, res, launches);
+        if (stored_only) {
+            if (!store || geopos) return FOORT_OK;
+            for (uint64_t g = 0; g < n; ++g) {
+                uint64_t at = 0;
+                if (!store->slot.get(PixelMap::key(px[g]), at)) return FOORT_OK;
+                res[g] = store->res[at];
+            }
+        } else if (store) {
+            rc = results_from_store(ctx, *store, px, res, launches);
         } else {
             rc = launch(ctx, px, res, launches);
         }
@@ -368,12 +391,53 @@ int run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs,
         }
         total += n;
         ++n_rounds;
+        ran = true;
+        return FOORT_OK;
+    }
+};
+
+int run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs, uint32_t n_images,
+        uint64_t* geodesics, uint32_t* rounds, uint32_t& launches, uint32_t& schedule) {
+    foort_run_desc desc;
+    if (foort_gpu_get_desc(ctx, &desc)) return FOORT_E_BADARG;
+    const bool geopos = (desc.diag_flags & FOORT_DIAG_GEODESIC_POSITION) != 0;
+    const std::vector<uint32_t> order = foort::diagnostic_order(desc.diag_flags, desc.value_diag);
+    Rounds R{ctx, meshes, outputs, n_images, geopos, order.empty() ? 0u : order[0]};
+    int rc = FOORT_OK;
+    ResultStore store;
+    schedule = FOORT_SCHEDULE_ROUNDS;
+    // A SimpleSquareMesh is its own single wave: without an adaptive mesh the waves are
+    // the rounds, and storing the results would only cost time.
+    bool adaptive = false;
+    for (uint32_t i = 0; i < n_images; ++i) adaptive = adaptive || foort_mesh_kind(meshes[i]) == FOORT_MESH_SUBDIVISION_V2;
+    if (adaptive && foort_ctx_schedule(ctx) == FOORT_SCHEDULE_WAVES && !geopos && foort_ctx_budget(ctx) == 0) {
+        // while a launch runs: the rounds whose results are all stored
+        auto replay = [&]() -> int {
+            bool ran = true;
+            while (ran) {
+                const int r = R.next(&store, launches, true, ran);
+                if (r) return r;
+            }
+            return FOORT_OK;
+        };
+        rc = integrate_waves(ctx, meshes, n_images, store, launches, replay);
+        if (rc == FOORT_OK) {
+            schedule = FOORT_SCHEDULE_WAVES;
+        } else if (rc != FOORT_E_UNSUPPORTED) {
+            return rc;
+        }
+    }
+    const ResultStore* from = schedule == FOORT_SCHEDULE_WAVES ? &store : nullptr;
+    for (;;) {
+        bool ran = false;
+        if ((rc = R.next(from, launches, false, ran))) return rc;
+        if (!ran) break;
     }
     if (outputs)
         for (uint32_t i = 0; i < n_images; ++i)
             if (outputs[i] && (rc = foort_output_finish(outputs[i]))) return rc;
-    if (geodesics) *geodesics = total;
-    if (rounds) *rounds = n_rounds;
+    if (geodesics) *geodesics = R.total;
+    if (rounds) *rounds = R.n_rounds;
     return FOORT_OK;
 }
 

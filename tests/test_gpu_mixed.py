@@ -254,6 +254,33 @@ def test_mixed_budget_and_cancel_paths(eng):
     assert np.any(res["err"] & (abi.ERR_BUDGET | abi.ERR_UNFINISHED))
 
 
+def test_integrate_async_returns_before_the_launch_ends(eng):
+    """foort_gpu_integrate_async returns once the launch is enqueued: on a launch of about
+    0.1 s (2,048 of the C2 run's pixels, ~66k steps each) the call takes a small part of
+    it, and foort_gpu_sync then waits for results equal to the synchronous call's."""
+    import time
+    import torch
+    f = np.load(os.path.join(GOLDEN, "c2_run.npz"))
+    px = np.zeros(2048, dtype=abi.PIXEL_DTYPE)
+    px["row"], px["col"], px["grid"] = f["row"][:2048], f["col"][:2048], 509
+    wl = workloads.c2(abi.PREC_MIXED)
+    with eng.Engine(wl.desc) as e:
+        ref = e.integrate(px)
+        d_px = torch.from_numpy(px.view(np.uint8).copy()).cuda()
+        d_out = torch.zeros(len(px) * abi.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.integrate_async(d_px.data_ptr(), len(px), d_out.data_ptr())
+        t_call = time.perf_counter() - t0
+        e.sync()
+        t_all = time.perf_counter() - t0
+        got = np.frombuffer(d_out.cpu().numpy().tobytes(), dtype=abi.RESULT_DTYPE)
+    print(f"call {t_call * 1e3:.2f} ms, launch {t_all * 1e3:.1f} ms")
+    assert t_all > 0.03 and t_call < 0.25 * t_all, (t_call, t_all)
+    for name in abi.RESULT_DTYPE.names:
+        np.testing.assert_array_equal(got[name], ref[name], err_msg=name)
+
+
 # Manko-Novikov (a, alpha3): the reference's Test.cfg value alpha3 = 13, its default 5,
 # and a mild 1
 MN_SETS = {"alpha3_13": (0.94, 13.0), "alpha3_5": (0.9, 5.0), "alpha3_1": (0.7, 1.0)}
