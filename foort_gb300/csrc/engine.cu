@@ -878,7 +878,7 @@ const void* fp64_kernel(int metric_id, int integ) {
 // The launch counters and the per-image constants that foort_gpu_create() puts in
 // cudaMalloc'd memory live here in one statically declared device array instead. On the
 // host, foort_noalloc_scratch names that array only as a symbol: its device address on
-// the current device comes from cudaGetSymbolAddress, looked up once per device.
+// the current device comes from cudaGetSymbolAddress, looked up on every call.
 
 static_assert(sizeof(ImageConst) == 672, "FOORT_NOALLOC_SCRATCH_BYTES assumes 672-byte image constants");
 static_assert(kNumCtr * sizeof(unsigned long long) <= 256, "the counters take the first 256 bytes");
@@ -897,20 +897,22 @@ struct NoAllocDevice {
 std::mutex g_noalloc_mu;
 NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
 
-// Set-up of the current device, on its first call: the array's device address and the
-// SM count. Takes no stream operation.
+// The current device's array address and SM count. The address is looked up on every
+// call (cheap once the module is loaded): a context made anew after cudaDeviceReset loads
+// the module again, possibly elsewhere. The SM count is the device's and is kept. Takes
+// no stream operation.
 int noalloc_device(int dev, NoAllocDevice& out) {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     NoAllocDevice& d = g_noalloc_dev[dev];
-    if (!d.scratch) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, foort_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(foort_noalloc_scratch)");
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, foort_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(foort_noalloc_scratch)");
+    d.scratch = static_cast<unsigned char*>(p);
+    if (!d.num_sms) {
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaDeviceGetAttribute");
         d.num_sms = sms;
-        d.scratch = static_cast<unsigned char*>(p);
     }
     out = d;
     return FOORT_OK;
