@@ -123,11 +123,11 @@ def c2_sample(n=8000, seed=11):
 
 
 # Against the FP64-analytic oracle (every step in FP64 with the mixed kernel's
-# derivatives), plain r: on well-conditioned pixels (kappa <= 10) at least 98 % of end
-# points within 1e-6 and the median within 1e-7; a backward error (error / kappa, in units
-# of the screen) with p99 within 1e-6 and a median no larger than that of the plain FP64
-# kernel, whose finite differences (h = 1e-7) keep fewer digits where the metric is nearly
-# flat. In log-r mode the backward error is as small as in plain r, but the reference's
+# derivatives), plain r: on well-conditioned pixels (kappa <= 10) the p99 of the endpoint
+# error within 1e-6 (at least 98 % of end points within it) and the median within 1e-7;
+# a backward error (error / kappa, in units of the screen) with p99 within 1e-6 and a
+# median no larger than that of the plain FP64 kernel, whose finite differences
+# (h = 1e-7) keep fewer digits where the metric is nearly flat. In log-r mode the backward error is as small as in plain r, but the reference's
 # finite differences are far better there (h = 1e-7 in ln r is a relative step) and the
 # shipped log-r view is mostly ill-conditioned pixels: there the median within 1e-6, 80 %
 # of well-conditioned pixels within 1e-6 and the backward error's p99 within 1e-6.
@@ -151,7 +151,7 @@ def test_mixed_against_the_fp64_analytic_oracle(eng, case):
     if wl.desc.rlog:
         assert rm["all"]["median"] <= 1e-6 and w["frac_le_1e-6"] >= 0.8, (rm["all"], w)
     else:
-        assert w["frac_le_1e-6"] >= 0.98 and w["median"] <= 1e-7, w
+        assert w["p99"] <= 1e-6 and w["frac_le_1e-6"] >= 0.98 and w["median"] <= 1e-7, w
         assert b["median"] <= bf["median"], (b, bf)
 
 
