@@ -69,11 +69,11 @@ OPS_PER_EXTRA_VERLET_RHS = 380
 # by its geodesics
 DRAM_BYTES_PER_GEODESIC = {("kerr", "rk4"): 120.4}
 # Executed thread instructions per geodesic step of the mixed kernel (ncu
-# smsp__inst_executed x 32 / steps): two lanes of ~929 each and one lane of 1,274 on a
-# 6,000-pixel sample of the C2 grid; Johannsen Verlet (one lane) 1,759 on 20,000 pixels
+# smsp__inst_executed x 32 / steps): two lanes of ~929 each and one lane of 1,270 on a
+# 6,000-pixel sample of the C2 grid; Johannsen Verlet (one lane) 1,754 on 20,000 pixels
 # of C4's. With the GPU's issue rate (one warp instruction per cycle on each of its
 # 4 x 152 sub-partitions) they give the fraction of issue slots the path fills.
-EXEC_INSTR_PER_STEP = {("kerr", "rk4", 2): 1857, ("kerr", "rk4", 1): 1274, ("johannsen", "verlet", 1): 1759}
+EXEC_INSTR_PER_STEP = {("kerr", "rk4", 2): 1857, ("kerr", "rk4", 1): 1270, ("johannsen", "verlet", 1): 1754}
 SUBPARTITIONS = 4
 # runs of more geodesics take the FP64 legs on a seeded sample (1 %, at least 20,000)
 FP64_SAMPLE_ABOVE = 60000
