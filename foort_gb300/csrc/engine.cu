@@ -28,7 +28,9 @@ struct foort_ctx {
     // Pinned, so that the copy of the counters after a launch does not hold the host until
     // the kernel ends (a copy into pageable memory returns only once it is done).
     unsigned long long* h_ctr = nullptr;
-    foort_result* h_stage = nullptr;  // pinned results of a run's launch in flight
+    // pinned pixels and results of foort_gpu_run's launches (foort_ctx_stage)
+    foort_pixel* h_stage_px = nullptr;
+    foort_result* h_stage = nullptr;
     uint64_t stage_cap = 0;
     int32_t* h_cancel = nullptr;
     int32_t* d_cancel = nullptr;
@@ -754,10 +756,27 @@ void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule
     ctx->run_launches = launches;
     ctx->run_schedule = schedule;
 }
+// Pinned room for n pixels and n results, kept by the context from run to run.
+int foort_ctx_stage(foort_ctx* ctx, uint64_t n, foort_pixel** px, foort_result** res) {
+    if (n > ctx->stage_cap) {
+        if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+        if (ctx->h_stage_px) cudaFreeHost(ctx->h_stage_px);
+        ctx->h_stage = nullptr;
+        ctx->h_stage_px = nullptr;
+        ctx->stage_cap = 0;
+        CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_stage), n * sizeof(foort_result), cudaHostAllocDefault));
+        CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_stage_px), n * sizeof(foort_pixel), cudaHostAllocDefault));
+        ctx->stage_cap = n;
+    }
+    if (px) *px = ctx->h_stage_px;
+    if (res) *res = ctx->h_stage;
+    return FOORT_OK;
+}
 // foort_gpu_integrate in two halves, for foort_gpu_run to work on the host while a launch
 // runs: begin enqueues the copy of n pixels from host memory, the launch and the copy of
-// the results into pinned memory, and returns; end waits for them and copies the results
-// out. Nothing else may launch on the context in between.
+// the results into the pinned staging, and returns; end waits for them and copies the
+// results out (out == NULL: they stay in the staging, foort_ctx_stage). px may be the
+// staging's own pixels. Nothing else may launch on the context in between.
 int foort_ctx_integrate_begin(foort_ctx* ctx, const foort_pixel* px, uint64_t n) {
     if (!ctx) return fail(nullptr, FOORT_E_BADARG, "ctx is NULL");
     if (n && !px) return fail(ctx, FOORT_E_BADARG, "NULL pixel buffer");
@@ -768,11 +787,8 @@ int foort_ctx_integrate_begin(foort_ctx* ctx, const foort_pixel* px, uint64_t n)
     if (rc != FOORT_OK && rc != FOORT_E_BUDGET && rc != FOORT_E_CANCELLED) return rc;
     if ((rc = ensure_capacity(ctx, n))) return rc;
     if (n > ctx->stage_cap) {
-        if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
-        ctx->h_stage = nullptr;
-        ctx->stage_cap = 0;
-        CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_stage), n * sizeof(foort_result), cudaHostAllocDefault));
-        ctx->stage_cap = n;
+        if (px == ctx->h_stage_px) return fail(ctx, FOORT_E_BADARG, "staged pixels beyond the staging");
+        if ((rc = foort_ctx_stage(ctx, n, nullptr, nullptr))) return rc;
     }
     cudaStream_t st = ctx->stream;
     if (n) CK(cudaMemcpyAsync(ctx->d_px, px, n * sizeof(foort_pixel), cudaMemcpyHostToDevice, st));
@@ -782,7 +798,7 @@ int foort_ctx_integrate_begin(foort_ctx* ctx, const foort_pixel* px, uint64_t n)
 }
 int foort_ctx_integrate_end(foort_ctx* ctx, foort_result* out, uint64_t n) {
     const int rc = finish(ctx);
-    if (n && (rc == FOORT_OK || rc == FOORT_E_BUDGET || rc == FOORT_E_CANCELLED))
+    if (out && n && (rc == FOORT_OK || rc == FOORT_E_BUDGET || rc == FOORT_E_CANCELLED))
         std::memcpy(out, ctx->h_stage, n * sizeof(foort_result));
     return rc;
 }
@@ -809,6 +825,7 @@ void foort_gpu_destroy(foort_ctx* ctx) {
     if (ctx->h_cancel) cudaFreeHost(ctx->h_cancel);
     if (ctx->h_ctr) cudaFreeHost(ctx->h_ctr);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    if (ctx->h_stage_px) cudaFreeHost(ctx->h_stage_px);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

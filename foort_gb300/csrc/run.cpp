@@ -34,17 +34,18 @@ uint64_t foort_ctx_budget(const foort_ctx* ctx);
 uint64_t foort_ctx_lookahead(const foort_ctx* ctx);
 void foort_ctx_set_run_info(foort_ctx* ctx, uint32_t launches, uint32_t schedule);
 void foort_ctx_launched(foort_ctx* ctx, const foort_pixel* px, uint64_t n, bool first);
+int foort_ctx_stage(foort_ctx* ctx, uint64_t n, foort_pixel** px, foort_result** res);
 int foort_ctx_integrate_begin(foort_ctx* ctx, const foort_pixel* px, uint64_t n);
 int foort_ctx_integrate_end(foort_ctx* ctx, foort_result* out, uint64_t n);
 }
 
 namespace {
 
-// The pixels of every unfinished mesh, image after image; count[i] pixels of image i
-// (0 for a finished mesh). any: some mesh is unfinished.
-int gather(foort_mesh* const* meshes, uint32_t n_images, std::vector<foort_pixel>& px, std::vector<uint64_t>& count,
-           bool& any) {
-    uint64_t n = 0;
+// How many pixels each unfinished mesh hands out this round: count[i] of image i (0 for a
+// finished mesh), n in all. any: some mesh is unfinished.
+int count_pixels(foort_mesh* const* meshes, uint32_t n_images, std::vector<uint64_t>& count, bool& any,
+                 uint64_t& n) {
+    n = 0;
     any = false;
     for (uint32_t i = 0; i < n_images; ++i) {
         const int fin = foort_mesh_is_finished(meshes[i]);
@@ -53,11 +54,15 @@ int gather(foort_mesh* const* meshes, uint32_t n_images, std::vector<foort_pixel
         any = any || !fin;
         n += count[i];
     }
-    px.resize(n);
+    return FOORT_OK;
+}
+
+// Those pixels, image after image, into px.
+int fill_pixels(foort_mesh* const* meshes, uint32_t n_images, const std::vector<uint64_t>& count, foort_pixel* px) {
     uint64_t k = 0;
     for (uint32_t i = 0; i < n_images; ++i) {
         if (foort_mesh_is_finished(meshes[i])) continue;
-        const int rc = foort_mesh_get_pixels(meshes[i], i, px.data() + k);
+        const int rc = foort_mesh_get_pixels(meshes[i], i, px + k);
         if (rc) return rc;
         k += count[i];
     }
@@ -65,35 +70,44 @@ int gather(foort_mesh* const* meshes, uint32_t n_images, std::vector<foort_pixel
 }
 
 // Map from a pixel (image, grid cell) to an index: open addressing with linear probing
-// over a power-of-two table kept at most half full. For C5's 182k results, one insert and
-// two lookups each take 22 ms on an x86-64 host core against std::unordered_map's 42 ms.
+// over a power-of-two table of (key, value) slots kept at most half full, sized ahead of
+// each batch of inserts (reserve). For C5's 187k results, one insert and two lookups each
+// take 10 ms on an x86-64 host core (20 ms with keys and values in separate arrays and
+// growth by doubling, 42 ms with std::unordered_map).
 class PixelMap {
   public:
     static uint64_t key(const foort_pixel& p) { return (static_cast<uint64_t>(p.image) << 42) | (p.row * p.grid + p.col); }
     bool get(uint64_t k, uint64_t& v) const {
-        if (keys_.empty()) return false;
+        if (slots_.empty()) return false;
         for (uint64_t i = mix(k) & mask_;; i = (i + 1) & mask_) {
-            if (keys_[i] == k) {
-                v = vals_[i];
+            const Slot& s = slots_[i];
+            if (s.key == k) {
+                v = s.val;
                 return true;
             }
-            if (keys_[i] == kEmpty) return false;
+            if (s.key == kEmpty) return false;
         }
     }
     bool has(uint64_t k) const {
         uint64_t v;
         return get(k, v);
     }
+    // Room for n entries in all without a rehash.
+    void reserve(uint64_t n) {
+        uint64_t cap = 64;
+        while (cap < 2 * n) cap *= 2;
+        if (cap > slots_.size()) rehash(cap);
+    }
     void put(uint64_t k, uint64_t v) {
-        if (2 * (size_ + 1) > keys_.size()) rehash(std::max<uint64_t>(64, 2 * keys_.size()));
+        if (2 * (size_ + 1) > slots_.size()) rehash(std::max<uint64_t>(64, 2 * slots_.size()));
         for (uint64_t i = mix(k) & mask_;; i = (i + 1) & mask_) {
-            if (keys_[i] == k) {
-                vals_[i] = v;
+            Slot& s = slots_[i];
+            if (s.key == k) {
+                s.val = v;
                 return;
             }
-            if (keys_[i] == kEmpty) {
-                keys_[i] = k;
-                vals_[i] = v;
+            if (s.key == kEmpty) {
+                s = Slot{k, v};
                 ++size_;
                 return;
             }
@@ -101,6 +115,9 @@ class PixelMap {
     }
 
   private:
+    struct Slot {
+        uint64_t key, val;
+    };
     static constexpr uint64_t kEmpty = ~0ull;  // no pixel has this key (image < 2^22)
     static uint64_t mix(uint64_t x) {  // the splitmix64 finaliser
         x ^= x >> 30;
@@ -110,15 +127,14 @@ class PixelMap {
         return x ^ (x >> 31);
     }
     void rehash(uint64_t cap) {
-        std::vector<uint64_t> k(cap, kEmpty), v(cap);
-        std::swap(k, keys_);
-        std::swap(v, vals_);
+        std::vector<Slot> old(cap, Slot{kEmpty, 0});
+        std::swap(old, slots_);
         mask_ = cap - 1;
         size_ = 0;
-        for (uint64_t i = 0; i < k.size(); ++i)
-            if (k[i] != kEmpty) put(k[i], v[i]);
+        for (const Slot& s : old)
+            if (s.key != kEmpty) put(s.key, s.val);
     }
-    std::vector<uint64_t> keys_, vals_;
+    std::vector<Slot> slots_;
     uint64_t mask_ = 0, size_ = 0;
 };
 
@@ -171,6 +187,7 @@ int lookahead_candidates(foort_mesh* const* waves, uint32_t n_images, const std:
         return FOORT_OK;
     }
     PixelMap now;
+    now.reserve(todo.size());
     for (const foort_pixel& p : todo) now.put(PixelMap::key(p), 0);
     std::vector<foort_pixel> cand;
     for (uint32_t i = 0; i < n_images; ++i) {
@@ -254,6 +271,8 @@ int integrate_waves(foort_ctx* ctx, foort_mesh* const* meshes, uint32_t n_images
                 if (fits) todo.insert(todo.end(), spec.begin(), spec.end());
             }
             if ((rc = launch_overlapped(ctx, todo, got, launches, during))) break;
+            store.slot.reserve(store.res.size() + todo.size());
+            store.res.reserve(store.res.size() + todo.size());
             for (uint64_t g = 0; g < todo.size(); ++g) {
                 store.slot.put(PixelMap::key(todo[g]), store.res.size());
                 store.res.push_back(got[g]);
@@ -316,34 +335,48 @@ struct Rounds {
     std::vector<uint64_t> count;
 
     // One round over every unfinished mesh. Its results come from `store` where given
-    // (with one launch for the pixels it lacks), else from a launch. stored_only: run the
-    // round only if the store holds all of its results (ran tells), and never launch.
+    // (with one launch for the pixels it lacks), else from a launch, whose pixels and
+    // results stay in the context's pinned staging. stored_only: run the round only if the
+    // store holds all of its results (ran tells), and never launch.
     int next(const ResultStore* store, uint32_t& launches, bool stored_only, bool& ran) {
         ran = false;
         if (done) return FOORT_OK;
         bool any = false;
+        uint64_t n = 0;
         count.resize(n_images);
-        int rc = gather(meshes, n_images, px, count, any);
+        int rc = count_pixels(meshes, n_images, count, any, n);
         if (rc) return rc;
         if (!any) {
             done = true;
             return FOORT_OK;
         }
-        const uint64_t n = px.size();
-        res.resize(n);
-        if (stored_only) {
-            if (!store || geopos) return FOORT_OK;
-            for (uint64_t g = 0; g < n; ++g) {
-                uint64_t at = 0;
-                if (!store->slot.get(PixelMap::key(px[g]), at)) return FOORT_OK;
-                res[g] = store->res[at];
+        foort_pixel* P = nullptr;
+        foort_result* Rs = nullptr;
+        if (store) {
+            px.resize(n);
+            res.resize(n);
+            P = px.data();
+            Rs = res.data();
+            if ((rc = fill_pixels(meshes, n_images, count, P))) return rc;
+            if (stored_only) {
+                if (geopos) return FOORT_OK;
+                for (uint64_t g = 0; g < n; ++g) {
+                    uint64_t at = 0;
+                    if (!store->slot.get(PixelMap::key(P[g]), at)) return FOORT_OK;
+                    Rs[g] = store->res[at];
+                }
+            } else if ((rc = results_from_store(ctx, *store, px, res, launches))) {
+                return rc;
             }
-        } else if (store) {
-            rc = results_from_store(ctx, *store, px, res, launches);
         } else {
-            rc = launch(ctx, px, res, launches);
+            if (stored_only) return FOORT_OK;
+            if ((rc = foort_ctx_stage(ctx, n, &P, &Rs))) return rc;
+            if ((rc = fill_pixels(meshes, n_images, count, P))) return rc;
+            foort_ctx_launched(ctx, P, n, launches == 0);
+            ++launches;
+            if ((rc = foort_ctx_integrate_begin(ctx, P, n))) return rc;
+            if ((rc = foort_ctx_integrate_end(ctx, nullptr, n))) return rc;
         }
-        if (rc != FOORT_OK) return rc;
         // GeodesicPosition: a second pass records the positions (foort_gpu_positions)
         std::vector<uint64_t> counts, first;
         std::vector<double> points;
@@ -351,10 +384,10 @@ struct Rounds {
             counts.resize(n);
             first.resize(n);
             uint64_t total_pts = 0;
-            if ((rc = foort_gpu_positions(ctx, px.data(), n, res.data(), counts.data(), nullptr, 0, &total_pts)))
+            if ((rc = foort_gpu_positions(ctx, P, n, Rs, counts.data(), nullptr, 0, &total_pts)))
                 return rc;
             points.resize(4 * std::max<uint64_t>(total_pts, 1));
-            if ((rc = foort_gpu_positions(ctx, px.data(), n, res.data(), counts.data(), points.data(), total_pts,
+            if ((rc = foort_gpu_positions(ctx, P, n, Rs, counts.data(), points.data(), total_pts,
                                           &total_pts)))
                 return rc;
             uint64_t s = 0;
@@ -370,20 +403,20 @@ struct Rounds {
                 // getFinalDataVal: (theta, phi) of the last kept position (Diagnostics.cpp:304-309)
                 for (uint64_t g = 0; g < count[i]; ++g) {
                     const uint64_t q = k + g;
-                    double v[2] = {res[q].pos[2], res[q].pos[3]};
+                    double v[2] = {Rs[q].pos[2], Rs[q].pos[3]};
                     if (counts[q]) {
                         v[0] = points[4 * (first[q] + counts[q] - 1) + 2];
                         v[1] = points[4 * (first[q] + counts[q] - 1) + 3];
                     }
                     if ((rc = foort_mesh_geodesic_finished(meshes[i], g, v, 2))) return rc;
                 }
-            } else if ((rc = foort_mesh_set_results(meshes[i], res.data() + k, count[i]))) {
+            } else if ((rc = foort_mesh_set_results(meshes[i], Rs + k, count[i]))) {
                 return rc;
             }
             if (outputs && outputs[i]) {
-                rc = geopos ? foort_output_round_positions(outputs[i], px.data() + k, res.data() + k, count[i],
+                rc = geopos ? foort_output_round_positions(outputs[i], P + k, Rs + k, count[i],
                                                            counts.data() + k, points.data() + 4 * (k < n ? first[k] : 0))
-                            : foort_output_round(outputs[i], px.data() + k, res.data() + k, count[i]);
+                            : foort_output_round(outputs[i], P + k, Rs + k, count[i]);
                 if (rc) return rc;
             }
             if ((rc = foort_mesh_end_current_loop(meshes[i]))) return rc;
