@@ -30,8 +30,8 @@ struct G5T {
 // gives NaN where 1/x is infinite, and so for any |x| below FLT_MIN, which the .ftz
 // forms flush to 0: the factors are r - r_+, r - r_-, sin(theta), Sigma, r and the like,
 // below 1.2e-38 only within that distance of a horizon, a pole or the origin, where the
-// state turns non-finite with either value. Passing the infinity through cost C2 1.2 % on
-// GB300.
+// state turns non-finite with either value. Passing the infinity through cost 1.2 % on
+// GB300 in the Kerr a = 0.99 adaptive run (509² grid, 26,547 geodesics).
 FOORT_HD float rcp(float x) {
 #ifdef __CUDA_ARCH__
     float r0;
@@ -84,7 +84,8 @@ struct MixedMetric {
 // kInline: inline the body into each RK4 stage, or call it. Calling keeps large bodies
 // (Johannsen, ~300 temporaries) out of the register allocation of the stepping loop.
 // Kerr is inlined: with branch-free reciprocals its four copies fit the instruction
-// cache, and C2's five rounds take 695 ms inlined against 786 ms called on GB300.
+// cache, and the five rounds of the Kerr a = 0.99 adaptive run (509² grid, 26,547 geodesics)
+// take 695 ms inlined against 786 ms called on GB300.
 #define FOORT_DEFINE_MIXED_METRIC(ID, BODY, INL)                                                   \
     template <>                                                                                    \
     struct MixedMetric<ID> {                                                                       \

@@ -304,7 +304,7 @@ __device__ __forceinline__ void persistent_loop(const LaunchArgs& A, const RunCo
                         } else {
                             idx = my;
                             // i and cnt start at 0 as literals: copying them from the record
-                            // made the C4 kernel 3 % slower on GB300
+                            // made the Johannsen Verlet kernel 3 % slower on GB300
                             L.gp = (A.gp_plan && !odd && A.gp_plan[my].M > 0 && A.gp_plan[my].j > 0)
                                        ? GeoposRec{A.gp_plan[my].dst, A.gp_plan[my].j, A.gp_plan[my].M, 0, 0}
                                        : GeoposRec{nullptr, 1, 0, 0, 0};

@@ -9,15 +9,15 @@
 // Main.cpp:410). Images advance in lockstep, so a round is one launch over all images.
 //
 // Level waves (FOORT_SCHEDULE_WAVES). A launch lasts as long as its slowest geodesic, and
-// on the adaptive mesh's rounds that is most of the launch: C2's geodesics all take
-// 66,000-71,000 steps, so a round of 1,079 geodesics takes as long as one of 16,384. With
-// unlimited MaxPixels the mesh's pixel set is fixed by the values alone
-// (foort_mesh_create_waves), and it splits into one wave per subdivision level, each
-// depending only on the results of the waves before. The run integrates the waves first,
-// a wave's launch also taking the next wave's candidates (foort_mesh_lookahead) while it
-// stays within the context's lookahead cap (C2: two launches where the reference has five
-// rounds), then replays the meshes' rounds from the stored results, so meshes and output
-// files see the reference's rounds. With a finite MaxPixels an image's waves stop at that
+// on the adaptive mesh's rounds that is most of the launch: in the Kerr a = 0.99 run on a
+// 509² grid the geodesics all take 66,000-71,000 steps, so a round of 1,079 geodesics
+// takes as long as one of 16,384. With unlimited MaxPixels the mesh's pixel set is fixed
+// by the values alone (foort_mesh_create_waves), and it splits into one wave per
+// subdivision level, each depending only on the results of the waves before. The run
+// integrates the waves first, a wave's launch also taking the next wave's candidates
+// (foort_mesh_lookahead) while it stays within the context's lookahead cap (that run: two
+// launches where the reference has five rounds), then replays the meshes' rounds from the
+// stored results, so meshes and output files see the reference's rounds. With a finite MaxPixels an image's waves stop at that
 // budget, and its rounds integrate what the waves did not. While a wave's launch runs, the
 // host replays the rounds whose results are already stored.
 #include <algorithm>
@@ -71,9 +71,10 @@ int fill_pixels(foort_mesh* const* meshes, uint32_t n_images, const std::vector<
 
 // Map from a pixel (image, grid cell) to an index: open addressing with linear probing
 // over a power-of-two table of (key, value) slots kept at most half full, sized ahead of
-// each batch of inserts (reserve). For C5's 187k results, one insert and two lookups each
-// take 10 ms on an x86-64 host core (20 ms with keys and values in separate arrays and
-// growth by doubling, 42 ms with std::unordered_map).
+// each batch of inserts (reserve). For the 187k results of a Kerr a = 0.998 run on a
+// 4097² grid, one insert and two lookups each take 10 ms on an x86-64 host core (20 ms
+// with keys and values in separate arrays and growth by doubling, 42 ms with
+// std::unordered_map).
 class PixelMap {
   public:
     static uint64_t key(const foort_pixel& p) { return (static_cast<uint64_t>(p.image) << 42) | (p.row * p.grid + p.col); }
