@@ -20,6 +20,9 @@ struct foort_ctx {
     std::vector<foort_result> stage_res;
     bool pending = false;
     uint64_t pending_n = 0;
+    int64_t fail_at = -1;  // the launch (0-based) that reports fail_code instead of running
+    int fail_code = 0;
+    uint64_t calls = 0;
 };
 
 namespace {
@@ -68,6 +71,10 @@ uint64_t fake_ctx_launches(const foort_ctx* c) { return c->launch_sizes.size(); 
 uint64_t fake_ctx_launch_size(const foort_ctx* c, uint64_t k) { return c->launch_sizes[k]; }
 uint32_t fake_ctx_run_schedule(const foort_ctx* c) { return c->run_schedule; }
 uint32_t fake_ctx_run_launches(const foort_ctx* c) { return c->run_launches; }
+void fake_ctx_fail_at(foort_ctx* c, int64_t launch, int code) {
+    c->fail_at = launch;
+    c->fail_code = code;
+}
 
 // ---- what run.cpp calls
 uint32_t foort_ctx_schedule(const foort_ctx* c) { return c->schedule; }
@@ -93,6 +100,7 @@ int foort_ctx_stage(foort_ctx* c, uint64_t n, foort_pixel** px, foort_result** r
 }
 int foort_ctx_integrate_begin(foort_ctx* c, const foort_pixel* px, uint64_t n) {
     if (c->pending) return FOORT_E_BADARG;  // one launch in flight at a time
+    if (static_cast<int64_t>(c->calls++) == c->fail_at) return c->fail_code;
     if (n > c->stage_res.size()) {
         if (px == c->stage_px.data()) return FOORT_E_BADARG;
         c->stage_px.resize(n);
@@ -115,6 +123,7 @@ int foort_gpu_get_desc(const foort_ctx* c, foort_run_desc* d) {
 }
 int foort_gpu_integrate(foort_ctx* c, const foort_pixel* px, uint64_t n, foort_result* out) {
     if (c->pending) return FOORT_E_BADARG;
+    if (static_cast<int64_t>(c->calls++) == c->fail_at) return c->fail_code;
     compute(px, n, out);
     return FOORT_OK;
 }

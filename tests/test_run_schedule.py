@@ -40,6 +40,7 @@ def lib(tmp_path_factory):
     for f in ("fake_ctx_run_schedule", "fake_ctx_run_launches"):
         getattr(L, f).restype = u32
         getattr(L, f).argtypes = [vp]
+    L.fake_ctx_fail_at.argtypes = [vp, C.c_int64, C.c_int]
     L.foort_mesh_create_v2.argtypes = [u64, u64, C.c_int32, u64, C.c_int32, u32, u32, C.POINTER(vp)]
     L.foort_mesh_create_simple.argtypes = [u64, u32, u32, C.POINTER(vp)]
     L.foort_mesh_destroy.argtypes = [vp]
@@ -49,11 +50,14 @@ def lib(tmp_path_factory):
     return L
 
 
-def run(L, meshes, diag, value, schedule, lookahead, outdir):
+def run(L, meshes, diag, value, schedule, lookahead, outdir, fail=None):
     """One foort_gpu_run over fresh meshes built from `meshes` ((kind, args) per image),
     with each image's files under outdir. Returns (geodesics, rounds, launch sizes, the
-    schedule it used)."""
+    schedule it used); with fail = (launch, code), that launch reports the error code and
+    the run's return code is returned instead."""
     ctx = L.fake_ctx_create(diag, value, schedule, lookahead)
+    if fail:
+        L.fake_ctx_fail_at(ctx, *fail)
     ms, outs = [], []
     try:
         for i, (kind, args) in enumerate(meshes):
@@ -73,6 +77,8 @@ def run(L, meshes, diag, value, schedule, lookahead, outdir):
         g, r = C.c_uint64(), C.c_uint32()
         rc = L.foort_gpu_run(ctx, (C.c_void_p * n)(*[m.value for m in ms]), (C.c_void_p * n)(*[o.value for o in outs]),
                              n, C.byref(g), C.byref(r))
+        if fail:
+            return rc, L.fake_ctx_run_launches(ctx)
         assert rc == 0, rc
         sizes = [L.fake_ctx_launch_size(ctx, k) for k in range(L.fake_ctx_launches(ctx))]
         assert L.fake_ctx_run_launches(ctx) == len(sizes)
@@ -129,3 +135,20 @@ def test_waves_write_the_round_by_round_files(lib, tmp_path, case):
                 assert len(got[2]) < r, (name, got[2], sizes)
         else:
             assert got[3] == abi.SCHEDULE_ROUNDS and got[2] == sizes
+
+
+@pytest.mark.parametrize("schedule,lookahead", [(abi.SCHEDULE_ROUNDS, 0), (abi.SCHEDULE_WAVES, 0),
+                                                (abi.SCHEDULE_WAVES, 4000)])
+@pytest.mark.parametrize("at", [0, 1, 2])
+def test_a_failing_launch_ends_the_run_with_its_code(lib, tmp_path, schedule, lookahead, at):
+    """A launch that reports an error (a stand-in for a CUDA failure, made on the host)
+    ends foort_gpu_run with that code under every schedule, including a launch whose host
+    side was replaying stored rounds meanwhile; the launches counted stop there."""
+    meshes, value = CASES["v2_fourcolor"]
+    rc, launches = run(lib, meshes, FC | EP | CR, value, schedule, lookahead, tmp_path / "out",
+                       fail=(at, abi.FOORT_E_CUDA))
+    ok = run(lib, meshes, FC | EP | CR, value, schedule, lookahead, tmp_path / "ok")
+    if at < len(ok[2]):
+        assert rc == abi.FOORT_E_CUDA and launches == at + 1, (rc, launches, ok[2])
+    else:
+        assert rc == 0
