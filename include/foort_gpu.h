@@ -585,7 +585,9 @@ int foort_timestamp_string(char* buf, uint64_t cap);
  * pixels of every unfinished mesh in one launch (foort_gpu_integrate), passes the
  * results to the meshes (Main.cpp:399) and output files (Main.cpp:400), and ends the
  * meshes' rounds (Main.cpp:410); the outputs are finished at the end. Optional
- * geodesics / rounds receive the totals. */
+ * geodesics / rounds receive the totals. The context keeps pinned host buffers for the
+ * pixels and results of its largest launch (136 bytes per geodesic) until
+ * foort_gpu_destroy. */
 int foort_gpu_run(foort_ctx* ctx, foort_mesh* const* meshes, foort_output* const* outputs, uint32_t n_images,
                   uint64_t* geodesics, uint32_t* rounds);
 
